@@ -1,0 +1,105 @@
+/*
+ * lcirs.h - C ABI of liblcirs.so, the GB300 engine for TripleLens'
+ * extended-source light curves (inverse-ray shooting, LightCurveIRS).
+ *
+ * The first six entry points keep the reference's ctypes ABI exactly
+ * (src/LightCurves/lcirs.cc:515-609; bound by Examples/ctypes_classes.py:128-193),
+ * so the reference's Python drivers load this library unchanged.  The object
+ * pointer is opaque.  As in the reference, calls are synchronous, return
+ * nothing, and report to stdout; GPU-side conditions are additionally
+ * readable through lcirs_last_status().
+ *
+ * The remaining entry points are additive.
+ */
+#ifndef TL_LCIRS_H
+#define TL_LCIRS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct LightCurveIRS LightCurveIRS;
+
+/* Replaces lcirs_new (src/LightCurves/lcirs.cc:517-537).  Lens a, b, th, m2,
+ * m3 (z1 = 0, z2 = (a,0), z3 = b e^{i th}, m1 = 1 - m2 - m3), source radius,
+ * light-curve length n, rays per source radius.  Computes the critical curve,
+ * caustics and image-plane grid on the GPU. */
+LightCurveIRS* lcirs_new(double a, double b, double th, double m2, double m3, double sourceSize,
+                         unsigned int lcLength, long pointsPerRadius);
+
+/* Replaces get_lc (src/LightCurves/lcirs.cc:539-549 -> lcbase.cc:40-52):
+ * point-source magnification at n points t = i/(n-1) into the curve. */
+void get_lc(LightCurveIRS* lcirs, double iniX, double iniY, double finX, double finY);
+
+/* Replaces get_lc_irs (src/LightCurves/lcirs.cc:552-562 -> 103-191):
+ * extended-source magnification at n+1 points t = i/n; prints the
+ * reference's per-point line "irs amplification: A and the count N and amp
+ * scale s". */
+void get_lc_irs(LightCurveIRS* lcirs, double iniX, double iniY, double finX, double finY);
+
+/* Replaces copy_lc (src/LightCurves/lcirs.cc:566-576): copies exactly n
+ * doubles (the first n points of the last curve). */
+void copy_lc(LightCurveIRS* lc, double* lcArray);
+
+/* Replaces set_limb_darkening (src/LightCurves/lcirs.cc:579-598): "linear"
+ * selects the v-normalised linear model (limbdarkeningmodel.cc:18-28), any
+ * other string the default A = 0.6, B = 0.4. */
+void set_limb_darkening(LightCurveIRS* lc, const char* model, double v);
+
+/* Replaces set_amoeba_printout (src/LightCurves/lcirs.cc:601-607): after each
+ * point of get_lc_irs, write "<prefix><i>" with one "ny,xleft,xright" line
+ * per filled row range (amoeba.cc:90-108), and the grid parameters as JSON to
+ * parFilename (lcirs.cc:479-512, including its "m3" field holding m2). */
+void set_amoeba_printout(LightCurveIRS* lc, const char* amoebaFilename, const char* parFilename);
+
+/* ---- additive entry points (no counterpart in the reference ABI) ---- */
+
+/* Frees an object (the reference has no destroy export). */
+void lcirs_delete(LightCurveIRS* lc);
+
+/* OR of the status bits of the points of the last curve (0 = clean):
+ * 1 seed overflow, 2 plane edge reached, 4 tile table full, 8 bounded wait
+ * expired, 16 wrong image count after retry, 32 bad input,
+ * 0x100 CUDA error. */
+unsigned int lcirs_last_status(LightCurveIRS* lc);
+
+/* Ray counts of the last get_lc_irs, n+1 entries. */
+void lcirs_copy_counts(LightCurveIRS* lc, uint64_t* counts);
+
+/* All n+1 magnifications of the last get_lc_irs (copy_lc stops at n). */
+void lcirs_copy_lc_full(LightCurveIRS* lc, double* out);
+
+/* Per-point status bits of the last get_lc_irs, n+1 entries. */
+void lcirs_copy_status(LightCurveIRS* lc, uint32_t* status);
+
+/* 0 silences the per-point stdout lines (default 1, as the reference). */
+void lcirs_set_verbose(LightCurveIRS* lc, int verbose);
+
+/* Grid of the object: corner_x, corner_y, top_x, top_y, size, h, ampScale,
+ * N (as double).  8 doubles. */
+void lcirs_grid(LightCurveIRS* lc, double* out8);
+
+/* Seeds of the last get_lc_irs: per point up to 64 (nx, ny) pixel pairs and
+ * their number.  seeds: (n+1)*64*2 int32, nseeds: n+1 int32. */
+void lcirs_copy_seeds(LightCurveIRS* lc, int32_t* seeds, int32_t* nseeds);
+
+/* Fill only: given explicit seed pixels for each of the n+1 points of the
+ * trajectory (same layout as lcirs_copy_seeds), compute counts and
+ * magnifications with the GPU fill kernel. */
+void lcirs_fill_from_seeds(LightCurveIRS* lc, double iniX, double iniY, double finX, double finY,
+                           const int32_t* seeds, const int32_t* nseeds);
+
+/* Ray statistics of the last get_lc_irs: rays evaluated, rays evaluated in
+ * FP64, tiles visited (3 x uint64 totals). */
+void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3);
+
+/* Ray-map precision: 0 = every ray in FP64 (irsSIMD order); 1 = FP32
+ * tile-relative map with an FP64 guard band at the limb (default). */
+void lcirs_set_precision(LightCurveIRS* lc, int mode);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,72 @@
+/*
+ * tl_batch.h - batched entry points of liblcirs.so (additive; no counterpart
+ * in the reference, whose API computes one light curve per call through
+ * lcirs_new/get_lc_irs, src/LightCurves/lcirs.cc:515-562).
+ *
+ * A batch holds many lenses and many straight trajectories (each on one of
+ * the lenses).  One run computes, for every trajectory with length n, the
+ * n+1 extended-source magnifications at t = i/n (the reference's
+ * getLCIRS sampling, lcirs.cc:117-120), in one seeds launch and one
+ * persistent fill launch.  Results are identical to calling get_lc_irs on
+ * each lens object.
+ *
+ * Lens parameter rows (8 doubles): a, b, th, m2, m3, rho, ld_v, ppr, where
+ * ld_v >= 0 selects the v-normalised linear limb darkening ("linear", v)
+ * and ld_v < 0 the reference's default model (A = 0.6, B = 0.4).
+ * Trajectory rows (4 doubles): x0, y0, x1, y1.
+ *
+ * Return values: >= 0 success (number of points for runs), < 0 error
+ * (-1 bad argument, -2 CUDA error).
+ */
+#ifndef TL_BATCH_H
+#define TL_BATCH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tl_batch tl_batch;
+
+tl_batch* tlb_new(void);
+void tlb_delete(tl_batch* b);
+
+/* Lens set-up on the GPU (critical curves, caustics, grids). */
+int tlb_set_lenses(tl_batch* b, int nlens, const double* params8);
+
+/* Uploads trajectories (host arrays) into device memory and plans the
+ * chunks; returns the number of points (sum of n+1). */
+long tlb_set_trajectories(tl_batch* b, int ntraj, const double* traj4, const int32_t* lens_idx,
+                          const uint32_t* n);
+
+/* Runs on device-resident inputs.  phase: 1 seeds kernel, 2 fill kernel,
+ * 3 both.  stream: a cudaStream_t or NULL for the engine's stream.  No host
+ * synchronisation. */
+int tlb_run_device(tl_batch* b, int phase, void* stream);
+
+/* Copies results to host arrays of size (number of points); any pointer may
+ * be NULL.  Synchronises the stream. */
+int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, void* stream);
+
+/* End to end from host buffers: set trajectories, run, download. */
+long tlb_run_host(tl_batch* b, int ntraj, const double* traj4, const int32_t* lens_idx,
+                  const uint32_t* n, double* amp, uint64_t* counts, uint32_t* status,
+                  void* stream);
+
+/* Totals of the last run: rays evaluated, rays evaluated in FP64, tiles
+ * visited, accepted rays (4 x uint64). */
+int tlb_stats(tl_batch* b, uint64_t* out4);
+
+/* Ray-map precision (0 FP64 everywhere, 1 FP32 + FP64 guard band) and fill
+ * launch shape (ctas <= 0 and cap_log2 <= 0 keep the current values). */
+int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads);
+
+/* Point-source magnifications (reference get_lc sampling t = i/(n-1)) of the
+ * current trajectories, n points each, written to amp (host). */
+long tlb_point_lc(tl_batch* b, double* amp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

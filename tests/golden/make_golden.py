@@ -1,0 +1,167 @@
+"""Generates the golden fixtures in tests/golden/ from the REFERENCE itself.
+
+Runs only where the reference sources are present: it builds the reference
+library with oracle/Makefile.ref (into oracle/_ref/, git-ignored) and drives
+it through its own ctypes ABI (lcirs_new / set_limb_darkening / get_lc_irs /
+copy_lc, ccc_new / get_ca / copy_cc_ca, img_new / get_images / copy_images).
+Ray counts are read from the reference's per-point stdout line
+"irs amplification: A and the count N ..." (lcirs.cc:176-177); the filled
+sets from its amoeba dump files (amoeba.cc:90-108).
+
+    python tests/golden/make_golden.py [--ref /path/to/TripleLens] [--c2]
+
+Each reference run happens in a child process (its stdout is C++ cout).
+The committed outputs are small .npz files; this script is kept beside them.
+"""
+import argparse
+import ctypes
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from triplelens_gb300 import workloads  # noqa: E402
+
+REF_LIBS = {
+    "nfc": os.path.join(ROOT, "oracle", "_ref", "liblcirs_ref_nfc.so"),
+    "fast": os.path.join(ROOT, "oracle", "_ref", "liblcirs_ref.so"),
+}
+
+
+def worker(spec):
+    """Child process: one reference light curve; counts go to stdout."""
+    L = ctypes.cdll.LoadLibrary(spec["lib"])
+    d = ctypes.c_double
+    L.lcirs_new.argtypes = [d] * 6 + [ctypes.c_uint, ctypes.c_long]
+    L.lcirs_new.restype = ctypes.c_void_p
+    L.get_lc_irs.argtypes = [ctypes.c_void_p] + [d] * 4
+    L.copy_lc.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.set_limb_darkening.argtypes = [ctypes.c_void_p, ctypes.c_char_p, d]
+    L.set_amoeba_printout.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]
+    a, b, th, m2, m3, rho, v, ppr = spec["lens"]
+    n = spec["n"]
+    o = L.lcirs_new(a, b, th, m2, m3, rho, n, int(ppr))
+    if v >= 0:
+        L.set_limb_darkening(o, b"linear", v)
+    else:
+        L.set_limb_darkening(o, b"default", 0.0)
+    if spec.get("amoeba"):
+        L.set_amoeba_printout(o, spec["amoeba"].encode(), (spec["amoeba"] + "pars.json").encode())
+    x0, y0, x1, y1 = spec["traj"]
+    L.get_lc_irs(o, x0, y0, x1, y1)
+    out = np.zeros(n)
+    L.copy_lc(o, out.ctypes.data_as(ctypes.c_void_p))
+    np.save(spec["amp_out"], out)
+
+
+def run_curve(lib, lens, traj, n, amoeba=None):
+    with tempfile.TemporaryDirectory() as td:
+        spec = {"lib": lib, "lens": [float(x) for x in lens], "traj": [float(x) for x in traj],
+                "n": int(n), "amp_out": os.path.join(td, "amp.npy"), "amoeba": amoeba}
+        r = subprocess.run([sys.executable, __file__, "--worker", json.dumps(spec)],
+                           capture_output=True, text=True, check=True)
+        counts = np.array([int(m) for m in re.findall(r"the count (\d+)", r.stdout)], np.uint64)
+        amps = np.load(spec["amp_out"])
+    assert len(counts) == n + 1, (len(counts), n)
+    return counts, amps
+
+
+def read_amoeba(path):
+    t = np.loadtxt(path, delimiter=",", dtype=np.int64, ndmin=2).reshape(-1, 3)
+    return t[np.lexsort((t[:, 1], t[:, 0]))]
+
+
+def ccc_and_images(lib, lens, positions):
+    L = ctypes.cdll.LoadLibrary(lib)
+    d = ctypes.c_double
+    L.ccc_new.argtypes = [d] * 5 + [ctypes.c_int]
+    L.ccc_new.restype = ctypes.c_void_p
+    L.get_ca.argtypes = [ctypes.c_void_p]
+    L.copy_cc_ca.argtypes = [ctypes.c_void_p] * 3
+    L.img_new.argtypes = [d] * 7
+    L.img_new.restype = ctypes.c_void_p
+    L.get_images.argtypes = [ctypes.c_void_p]
+    L.copy_images.argtypes = [ctypes.c_void_p] * 3
+    a, b, th, m2, m3 = lens[:5]
+    obj = L.ccc_new(a, b, th, m2, m3, 500)
+    L.get_ca(obj)
+    cc = np.zeros(3000, np.complex128)
+    ca = np.zeros(3000, np.complex128)
+    L.copy_cc_ca(obj, cc.ctypes.data_as(ctypes.c_void_p), ca.ctypes.data_as(ctypes.c_void_p))
+    roots = np.zeros((len(positions), 10), np.complex128)
+    isimg = np.zeros((len(positions), 10), np.bool_)
+    for k, (sx, sy) in enumerate(positions):
+        im = L.img_new(a, b, th, m2, m3, sx, sy)
+        L.get_images(im)
+        r = np.zeros(10, np.complex128)
+        f = np.zeros(10, np.bool_)
+        L.copy_images(im, r.ctypes.data_as(ctypes.c_void_p), f.ctypes.data_as(ctypes.c_void_p))
+        roots[k], isimg[k] = r, f
+    return cc, ca, roots, isimg
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--worker")
+    ap.add_argument("--c2", action="store_true", help="also the 5000-point config-2 curve")
+    args = ap.parse_args()
+    if args.worker:
+        worker(json.loads(args.worker))
+        return
+    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", "REF=" + args.ref], cwd=ROOT,
+                   check=True)
+
+    lens, traj, n = workloads.config1()
+    out = {"lens": lens, "traj": traj, "n": n}
+    for tag, v in (("uniform", 0.0), ("default", -1.0), ("linear05", 0.5)):
+        L2 = lens.copy()
+        L2[6] = v
+        for build, lib in REF_LIBS.items():
+            c, a = run_curve(lib, L2, traj, n)
+            out["counts_%s_%s" % (tag, build)] = c
+            out["amps_%s_%s" % (tag, build)] = a
+    with tempfile.TemporaryDirectory() as td:
+        L2 = lens.copy()
+        L2[6] = 0.0
+        run_curve(REF_LIBS["nfc"], L2, traj, n, amoeba=os.path.join(td, "amo_"))
+        pts = [0, 20, 50, 75, 100]
+        out["amoeba_points"] = np.array(pts)
+        for p in pts:
+            out["amoeba_%d" % p] = read_amoeba(os.path.join(td, "amo_%d" % p))
+        with open(os.path.join(td, "amo_pars.json")) as f:
+            out["pars_json"] = np.array(f.read())
+    rng = np.random.Generator(np.random.PCG64(7))
+    positions = rng.uniform(-1.0, 1.5, size=(64, 2))
+    cc, ca, roots, isimg = ccc_and_images(REF_LIBS["nfc"], lens, positions)
+    out.update(cc=cc, ca=ca, img_positions=positions, img_roots=roots, img_isimg=isimg)
+    np.savez_compressed(os.path.join(HERE, "config1.npz"), **out)
+    print("wrote config1.npz")
+
+    # config-2 lenses, short curves (201 points over the same 4 theta_E)
+    lenses, trajs, _ = workloads.config2(seed=11, n_curves=3)
+    c2 = {"lenses": lenses, "trajs": trajs, "n": 200}
+    for k in range(len(lenses)):
+        c, a = run_curve(REF_LIBS["nfc"], lenses[k], trajs[k], 200)
+        c2["counts_%d" % k], c2["amps_%d" % k] = c, a
+    np.savez_compressed(os.path.join(HERE, "config2_short.npz"), **c2)
+    print("wrote config2_short.npz")
+
+    if args.c2:
+        lenses, trajs, n = workloads.config2(seed=0, n_curves=1)
+        c, a = run_curve(REF_LIBS["nfc"], lenses[0], trajs[0], n)
+        np.savez_compressed(os.path.join(HERE, "config2_seed0.npz"), lenses=lenses, trajs=trajs,
+                            n=n, counts=c, amps=a)
+        print("wrote config2_seed0.npz")
+
+
+if __name__ == "__main__":
+    main()

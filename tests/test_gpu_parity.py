@@ -1,0 +1,192 @@
+"""GPU engine (bin/liblcirs.so, through its C ABI) against the oracle and the
+reference's golden fixtures.
+
+Parity levels:
+  * given identical seed pixels, ray counts are bit-exact (every point);
+  * seeds: the GPU's image solver follows the oracle's warm-start chain with
+    restarts every 16 points; seed sets are identical;
+  * full pipeline vs the reference: identical on every point whose image
+    decisions are not at the 1e-6 filter radius (the oracle flags those).
+Magnifications: exact for uniform sources (weights are exactly 1), within the
+stated tolerance for limb darkening (summation order differs).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from triplelens_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+CHUNK = 16          # tl::kChainChunk
+LD_RTOL_FP64 = 1e-12
+LD_RTOL_SPLIT = 1e-6
+
+
+def _lc(product_lib, lens, n, precision):
+    from triplelens_gb300.lcirs import LC_irs
+    lc = LC_irs(*lens[:5], lens[5], n, int(lens[7]), lib_path=product_lib)
+    lc.set_verbose(0)
+    lc.set_precision(precision)
+    if lens[6] >= 0:
+        lc.set_limb_darkening("linear", lens[6])
+    else:
+        lc.set_limb_darkening("default", 0.0)
+    return lc
+
+
+def _oracle(oracle_lib, lens, n, chunk=CHUNK):
+    o = oracle_lib.OracleIRS(*lens[:5], lens[5], n, int(lens[7]))
+    o.set_chain_chunk(chunk)
+    if lens[6] >= 0:
+        o.set_limb_darkening("linear", lens[6])
+    else:
+        o.set_limb_darkening("default", 0.0)
+    return o
+
+
+def _seed_sets(seeds, cnt):
+    return [set(map(tuple, seeds[i, :cnt[i]].tolist())) for i in range(len(cnt))]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("v", [0.0, -1.0, 0.5])
+def test_config1_full_pipeline(product_lib, oracle_lib, golden_c1, precision, v):
+    lens, traj, n = workloads.config1()
+    lens = lens.copy()
+    lens[6] = v
+    lc = _lc(product_lib, lens, n, precision)
+    lc.get_lc_irs(*traj)
+    assert lc.last_status() & ~0x10 == 0
+    counts, amps = lc.counts(), lc.lc_full()
+    o = _oracle(oracle_lib, lens, n)
+    oseeds, ocnt, fragile = o.lc_seeds(*traj)
+    gseeds, gcnt = lc.seeds()
+    assert _seed_sets(gseeds, gcnt) == _seed_sets(oseeds, ocnt)
+    oamps, ocounts = o.lc_irs(*traj)
+    assert np.array_equal(counts, ocounts)
+    tag = {0.0: "uniform", -1.0: "default", 0.5: "linear05"}[v]
+    ref = golden_c1["counts_%s_nfc" % tag]
+    robust = fragile == 0
+    assert np.array_equal(counts[robust], ref[robust])
+    if v == 0.0:
+        assert np.array_equal(amps, oamps)
+    else:
+        tol = LD_RTOL_FP64 if precision == 0 else LD_RTOL_SPLIT
+        assert np.max(np.abs(amps - oamps) / oamps) < tol
+    # copy_lc returns exactly n values
+    out = np.full(n + 4, -7.0)
+    lc.copy_lc(out)
+    assert np.array_equal(out[:n], amps[:n]) and np.all(out[n:] == -7.0)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fill_from_oracle_seeds_is_exact(product_lib, oracle_lib, precision):
+    lens, traj, n = workloads.config1()
+    lens = lens.copy()
+    lens[6] = 0.5
+    o = oracle_lib.OracleIRS(*lens[:5], lens[5], n, int(lens[7]))
+    o.set_limb_darkening("linear", 0.5)
+    seeds, cnt, _ = o.lc_seeds(*traj)       # reference chain (no restarts)
+    lc = _lc(product_lib, lens, n, precision)
+    lc.fill_from_seeds(*traj, seeds.astype(np.int32), cnt)
+    counts, amps = lc.counts(), lc.lc_full()
+    for p in range(n + 1):
+        x = traj[0] + (traj[2] - traj[0]) * (p / n)
+        y = traj[1] + (traj[3] - traj[1]) * (p / n)
+        a, c = o.fill(x, y, seeds[p, :cnt[p]])
+        assert counts[p] == c, p
+        tol = LD_RTOL_FP64 if precision == 0 else LD_RTOL_SPLIT
+        assert abs(amps[p] - a) <= tol * a, p
+
+
+def test_amoeba_dump_matches_reference(product_lib, golden_c1, tmp_path):
+    lens, traj, n = workloads.config1()
+    lens = lens.copy()
+    lens[6] = 0.0
+    lc = _lc(product_lib, lens, n, 1)
+    prefix = str(tmp_path / "amo_")
+    lc.set_amoeba_printout(prefix, str(tmp_path / "pars.json"))
+    lc.get_lc_irs(*traj)
+    for p in golden_c1["amoeba_points"]:
+        t = np.loadtxt(prefix + str(p), delimiter=",", dtype=np.int64, ndmin=2).reshape(-1, 3)
+        t = t[np.lexsort((t[:, 1], t[:, 0]))]
+        assert np.array_equal(t, golden_c1["amoeba_%d" % p]), p
+    with open(tmp_path / "pars.json") as f:
+        assert f.read() == str(golden_c1["pars_json"])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_config2_short_vs_reference(product_lib, oracle_lib, precision):
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_short.npz"))
+    n = int(z["n"])
+    for k in range(len(z["lenses"])):
+        L, t = z["lenses"][k], z["trajs"][k]
+        lc = _lc(product_lib, L, n, precision)
+        lc.get_lc_irs(*t)
+        counts = lc.counts()
+        o = _oracle(oracle_lib, L, n)
+        _, _, fragile = o.lc_seeds(*t)
+        ref = z["counts_%d" % k]
+        robust = fragile == 0
+        assert np.array_equal(counts[robust], ref[robust]), k
+        rel = np.abs(lc.lc_full()[:n] - z["amps_%d" % k]) / z["amps_%d" % k]
+        assert np.max(rel[robust[:n]]) < (LD_RTOL_FP64 if precision == 0 else LD_RTOL_SPLIT) + 1e-13
+
+
+def test_batch_matches_objects(product_lib):
+    from triplelens_gb300.batch import Batch
+    lenses, trajs, _ = workloads.config2(seed=5, n_curves=4, n_points=60)
+    b = Batch(product_lib)
+    b.set_lenses(lenses)
+    amp, cnt, st = b.run(trajs, np.arange(4), np.full(4, 60))
+    for k in range(4):
+        lc = _lc(product_lib, lenses[k], 60, 1)
+        lc.get_lc_irs(*trajs[k])
+        sl = slice(61 * k, 61 * (k + 1))
+        assert np.array_equal(cnt[sl], lc.counts())
+        assert np.array_equal(amp[sl], lc.lc_full())
+
+
+def test_point_source_curve(product_lib, oracle_lib):
+    lens, traj, n = workloads.config1()
+    lc = _lc(product_lib, lens, n, 1)
+    lc.get_lc(*traj)
+    out = np.zeros(n)
+    lc.copy_lc(out)
+    o = _oracle(oracle_lib, lens, n)
+    ref = o.lc_point(*traj)
+    assert np.max(np.abs(out - ref) / ref) < 1e-9
+
+
+def test_binary_lens_m3_zero(product_lib, oracle_lib):
+    # m3 == 0 selects the two-lens ray map (lcirs.cc:28-36)
+    lens = np.array([1.2, 0.9, 1.0, 0.3, 0.0, 0.01, 0.0, 60.0])
+    traj = np.array([-1.5, 0.05, 1.5, 0.15])
+    n = 40
+    lc = _lc(product_lib, lens, n, 1)
+    lc.get_lc_irs(*traj)
+    o = _oracle(oracle_lib, lens, n)
+    _, ocounts = o.lc_irs(*traj)
+    assert np.array_equal(lc.counts(), ocounts)
+
+
+def test_short_and_far_curves(product_lib, oracle_lib):
+    # n = 1 (two points) and a source far from the caustics (A close to 1)
+    lens = np.array([1.0, 1.0, 1.2, 0.1, 0.05, 0.02, 0.3, 40.0])
+    for traj, n in ((np.array([0.1, 0.2, 0.3, 0.1]), 1), (np.array([1.8, 1.9, 2.1, 1.7]), 5)):
+        lc = _lc(product_lib, lens, n, 1)
+        lc.get_lc_irs(*traj)
+        o = _oracle(oracle_lib, lens, n)
+        _, ocounts = o.lc_irs(*traj)
+        assert np.array_equal(lc.counts(), ocounts)
+
+
+def test_bad_input_reports_status(product_lib):
+    lens = np.array([1.0, 1.0, 1.2, 0.1, 0.05, 0.02, 0.3, 40.0])
+    lc = _lc(product_lib, lens, 3, 1)
+    lc.get_lc_irs(float("nan"), 0.0, 0.5, 0.5)
+    st = lc.status()
+    assert st[0] & 32 and lc.last_status() & 32
+    assert lc.counts()[0] == 0

@@ -1,0 +1,248 @@
+// batch_abi.cu - batched light curves (include/tl_batch.h): many lenses,
+// many trajectories, one seeds launch and one persistent fill launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <vector>
+
+#include "engine.h"
+#include "engine_host.h"
+#include "tl_batch.h"
+
+using tl::cx;
+
+struct tl_batch {
+  int nlens = 0;
+  tl::DevBuf specs, lenses, cc, ca;
+  std::vector<tl::DevLens> hlens;
+  int ntraj = 0;
+  long npoints = 0;
+  int njobs = 0;
+  tl::DevBuf trajs, jobs, points, seeds, out, amp;
+  std::vector<tl::Traj> htraj;
+  int precision = 1;
+  uint64_t stats[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+cudaStream_t pick(void* s) {
+  return s ? (cudaStream_t)s : tl::Engine::get().stream;
+}
+
+}  // namespace
+
+extern "C" {
+
+tl_batch* tlb_new(void) {
+  tl::Engine::get();
+  return new tl_batch();
+}
+
+void tlb_delete(tl_batch* b) {
+  if (!b) return;
+  for (tl::DevBuf* d : {&b->specs, &b->lenses, &b->cc, &b->ca, &b->trajs, &b->jobs, &b->points,
+                        &b->seeds, &b->out, &b->amp})
+    if (d->p) cudaFree(d->p);
+  delete b;
+}
+
+int tlb_set_lenses(tl_batch* b, int nlens, const double* p8) {
+  if (!b || nlens <= 0 || !p8) return -1;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  std::vector<tl::LensSpec> specs(nlens);
+  for (int i = 0; i < nlens; i++) {
+    const double* q = p8 + 8 * (size_t)i;
+    double A, B, I;
+    if (q[6] >= 0.0) {  // limbdarkeningmodel.cc:18-28
+      const double v = q[6];
+      const double i0 = 1.0 / ((1.0 - v / 3.0));
+      A = i0 * (1.0 - v);
+      B = i0 * v;
+      I = 1.0;
+    } else {  // limbdarkeningmodel.cc:8-15
+      A = 0.6;
+      B = 0.4;
+      I = 1.0 / (A + 2.0 / 3.0 * B);
+    }
+    specs[i] = tl::make_lens_spec(q[0], q[1], q[2], q[3], q[4], q[5], (long)q[7], A, B, I);
+  }
+  b->nlens = nlens;
+  void* ds = b->specs.need(sizeof(tl::LensSpec) * nlens);
+  void* dl = b->lenses.need(sizeof(tl::DevLens) * nlens);
+  void* dcc = b->cc.need(sizeof(cx) * tl::kBranches * tl::kCCLen * nlens);
+  void* dca = b->ca.need(sizeof(cx) * tl::kBranches * tl::kCCLen * nlens);
+  if (!ds || !dl || !dcc || !dca) return -2;
+  if (!E.check(cudaMemcpyAsync(ds, specs.data(), sizeof(tl::LensSpec) * nlens,
+                               cudaMemcpyHostToDevice, E.stream)))
+    return -2;
+  tl::launch_lens_setup((const tl::LensSpec*)ds, nlens, (tl::DevLens*)dl, (cx*)dcc, (cx*)dca,
+                        E.stream);
+  b->hlens.resize(nlens);
+  E.check(cudaMemcpyAsync(b->hlens.data(), dl, sizeof(tl::DevLens) * nlens,
+                          cudaMemcpyDeviceToHost, E.stream));
+  if (!E.check(cudaStreamSynchronize(E.stream))) return -2;
+  return nlens;
+}
+
+long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
+                          const uint32_t* n) {
+  if (!b || ntraj <= 0 || !t4 || !lens_idx || !n || b->nlens <= 0) return -1;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  b->htraj.resize(ntraj);
+  std::vector<tl::SeedJob> jobs;
+  long base = 0;
+  for (int i = 0; i < ntraj; i++) {
+    if (lens_idx[i] < 0 || lens_idx[i] >= b->nlens || n[i] == 0) return -1;
+    tl::Traj& T = b->htraj[i];
+    T.x0 = t4[4 * (size_t)i];
+    T.y0 = t4[4 * (size_t)i + 1];
+    T.x1 = t4[4 * (size_t)i + 2];
+    T.y1 = t4[4 * (size_t)i + 3];
+    T.n = n[i];
+    T.lens = lens_idx[i];
+    T.point_base = base;
+    const long np = (long)n[i] + 1;
+    for (long f = 0; f < np; f += tl::kChainChunk) {
+      tl::SeedJob j;
+      j.traj = i;
+      j.first = (int32_t)f;
+      j.count = (int32_t)std::min<long>(tl::kChainChunk, np - f);
+      j.pad = 0;
+      jobs.push_back(j);
+    }
+    base += np;
+  }
+  if (base >= (1L << 31)) return -1;
+  b->ntraj = ntraj;
+  b->npoints = base;
+  b->njobs = (int)jobs.size();
+  void* dt = b->trajs.need(sizeof(tl::Traj) * ntraj);
+  void* dj = b->jobs.need(sizeof(tl::SeedJob) * jobs.size());
+  void* dp = b->points.need(sizeof(tl::PointIn) * base);
+  void* dsd = b->seeds.need(sizeof(int32_t) * 2 * tl::kMaxSeeds * base);
+  void* dout = b->out.need(sizeof(tl::PointOut) * base);
+  if (!dt || !dj || !dp || !dsd || !dout) return -2;
+  E.check(cudaMemcpyAsync(dt, b->htraj.data(), sizeof(tl::Traj) * ntraj, cudaMemcpyHostToDevice,
+                          E.stream));
+  E.check(cudaMemcpyAsync(dj, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                          cudaMemcpyHostToDevice, E.stream));
+  if (!E.check(cudaStreamSynchronize(E.stream))) return -2;
+  return base;
+}
+
+int tlb_run_device(tl_batch* b, int phase, void* stream) {
+  if (!b || b->npoints <= 0) return -1;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  cudaStream_t st = pick(stream);
+  if (phase & 1)
+    tl::launch_seeds((const tl::SeedJob*)b->jobs.p, b->njobs, (const tl::Traj*)b->trajs.p,
+                     (const tl::DevLens*)b->lenses.p, (const cx*)b->ca.p, (tl::PointIn*)b->points.p,
+                     (int32_t*)b->seeds.p, (tl::PointOut*)b->out.p, st);
+  if (phase & 2) {
+    tl::Run R;
+    R.trajs = (tl::Traj*)b->trajs.p;
+    R.jobs = (tl::SeedJob*)b->jobs.p;
+    R.points = (tl::PointIn*)b->points.p;
+    R.seeds = (int32_t*)b->seeds.p;
+    R.out = (tl::PointOut*)b->out.p;
+    R.dump = nullptr;
+    R.dump_count = nullptr;
+    R.dump_cap = 0;
+    E.fill_on(R, (size_t)b->npoints, (const tl::DevLens*)b->lenses.p, b->precision, st);
+  }
+  return E.check(cudaGetLastError()) ? 0 : -2;
+}
+
+int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, void* stream) {
+  if (!b || b->npoints <= 0) return -1;
+  tl::Engine& E = tl::Engine::get();
+  cudaStream_t st = pick(stream);
+  std::vector<tl::PointOut> h(b->npoints);
+  if (!E.check(cudaMemcpyAsync(h.data(), b->out.p, sizeof(tl::PointOut) * b->npoints,
+                               cudaMemcpyDeviceToHost, st)))
+    return -2;
+  if (!E.check(cudaStreamSynchronize(st))) return -2;
+  for (int k = 0; k < 4; k++) b->stats[k] = 0;
+  for (int t = 0; t < b->ntraj; t++) {
+    const tl::Traj& T = b->htraj[t];
+    const double scale = b->hlens[T.lens].g.amp_scale;
+    for (long i = 0; i <= (long)T.n; i++) {
+      const tl::PointOut& o = h[T.point_base + i];
+      if (amp) amp[T.point_base + i] = ((double)o.wsum_fx / tl::kWsumScale) * scale;
+      if (counts) counts[T.point_base + i] = o.count;
+      if (status) status[T.point_base + i] = o.status;
+      b->stats[0] += o.rays_eval;
+      b->stats[1] += o.rays_fp64;
+      b->stats[2] += o.tiles;
+      b->stats[3] += o.count;
+    }
+  }
+  return 0;
+}
+
+long tlb_run_host(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
+                  const uint32_t* n, double* amp, uint64_t* counts, uint32_t* status,
+                  void* stream) {
+  long np = tlb_set_trajectories(b, ntraj, t4, lens_idx, n);
+  if (np < 0) return np;
+  int r = tlb_run_device(b, 3, stream);
+  if (r < 0) return r;
+  r = tlb_download(b, amp, counts, status, stream);
+  return r < 0 ? r : np;
+}
+
+int tlb_stats(tl_batch* b, uint64_t* out4) {
+  if (!b || !out4) return -1;
+  for (int k = 0; k < 4; k++) out4[k] = b->stats[k];
+  return 0;
+}
+
+int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads) {
+  if (!b) return -1;
+  if (precision >= 0) b->precision = precision;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  E.set_fill_config(fill_ctas, table_log2, threads);
+  return 0;
+}
+
+long tlb_point_lc(tl_batch* b, double* amp) {
+  if (!b || b->ntraj <= 0 || !amp) return -1;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  // point-source sampling uses n points per curve (t = i/(n-1)); reuse the
+  // IRS layout (n+1 slots per curve) and leave the last slot unused
+  std::vector<tl::SeedJob> jobs;
+  for (int t = 0; t < b->ntraj; t++) {
+    const uint32_t n = b->htraj[t].n;
+    for (uint32_t f = 0; f < n; f += tl::kChainChunk) {
+      tl::SeedJob j;
+      j.traj = t;
+      j.first = (int32_t)f;
+      j.count = (int32_t)std::min<uint32_t>(tl::kChainChunk, n - f);
+      j.pad = 0;
+      jobs.push_back(j);
+    }
+  }
+  tl::DevBuf dj;
+  void* djp = dj.need(sizeof(tl::SeedJob) * jobs.size());
+  double* da = (double*)b->amp.need(sizeof(double) * b->npoints);
+  if (!djp || !da) return -2;
+  E.check(cudaMemsetAsync(da, 0, sizeof(double) * b->npoints, E.stream));
+  E.check(cudaMemcpyAsync(djp, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                          cudaMemcpyHostToDevice, E.stream));
+  tl::launch_point_lc((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp, (int)jobs.size(),
+                      (const tl::DevLens*)b->lenses.p, da, E.stream);
+  E.check(cudaMemcpyAsync(amp, da, sizeof(double) * b->npoints, cudaMemcpyDeviceToHost, E.stream));
+  bool ok = E.check(cudaStreamSynchronize(E.stream));
+  cudaFree(djp);
+  return ok ? b->npoints : -2;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// engine.h - data layout and host entry points of the GB300 IRS engine.
+//
+// Device data (all in HBM, one copy per engine):
+//   DevLens[nlens]          lens, grid, limb darkening, caustic boxes
+//   caustics[nlens][6][500] caustic samples (tl::cx), branch-major
+//   Traj[ntraj]             light curves: lens index, end points, length
+//   SeedJob[njobs]          chunks of consecutive points of one curve
+//   PointIn[npoints]        source position + lens index of every point
+//   seeds[npoints][kMaxSeeds] seed pixels (int32 x, y)
+//   PointOut[npoints]       ray count, fixed-point weight sum, status, stats
+//   fill scratch            per resident CTA: tile hash table, work ring
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tl_math.h"
+
+namespace tl {
+
+constexpr int kMaxSeeds = 64;     // seed pixels kept per point
+constexpr int kChainChunk = 16;   // points per warm-start chain (seed kernel)
+
+// status bits of a point (PointOut::status)
+enum : uint32_t {
+  kStSeedOverflow = 1u << 0,   // more than kMaxSeeds seeds: surplus dropped
+  kStEdge = 1u << 1,           // fill touched column 1 or N-1 (plane edge)
+  kStTableFull = 1u << 2,      // tile table full: point was not completed
+  kStTimeout = 1u << 3,        // a bounded wait ran out
+  kStImageCount = 1u << 4,     // wrong image count after the cold retry
+  kStBadInput = 1u << 5,       // non-finite source position or grid
+};
+
+struct DevLens {
+  Lens L;
+  Grid g;
+  double rho, rho2;
+  double ld_a, ld_b;       // weight = ld_a + ld_b * sqrt(1 - r^2/rho^2)
+  cx box_min[kBranches];   // caustic boxes (lcirs.cc:39-48, accumulated)
+  cx box_max[kBranches];
+  int32_t ray_binary;      // m3 == 0: two-lens ray map (lcirs.cc:28-36)
+  int32_t ppr;
+};
+
+struct LensSpec {          // host-side input of the lens set-up kernel
+  double m1, m2, m3;       // m1 = 1 - m2 - m3 (lens.cc:13)
+  double z2x;              // z2 = (a, 0)
+  double z3x, z3y;         // z3 = (b cos th, b sin th), host libm (lens.cc:38)
+  double rho;
+  double ld_a, ld_b, intensity;
+  int64_t ppr;
+  int32_t is_binary_img;   // a == 0 || b == 0 || m3 == 0
+  int32_t pad;
+};
+
+// Host-side construction of a LensSpec from the reference's constructor
+// arguments (lens.cc:4-18, limbdarkeningmodel.cc:8-28).
+LensSpec make_lens_spec(double a, double b, double th, double m2, double m3, double rho,
+                        long ppr, double ld_a, double ld_b, double intensity);
+
+struct Traj {
+  double x0, y0, x1, y1;
+  uint32_t n;              // IRS points at t = i/n, i = 0..n (n+1 points)
+  int32_t lens;
+  int64_t point_base;      // flat index of point 0
+};
+
+struct SeedJob {
+  int32_t traj;
+  int32_t first;           // first point index within the curve
+  int32_t count;
+  int32_t pad;
+};
+
+struct PointIn {
+  double sx, sy;
+  int32_t lens;
+  int32_t pad;
+};
+
+struct PointOut {
+  uint64_t count;          // accepted rays
+  int64_t wsum_fx;         // sum of weights, fixed point (units of 2^-32)
+  uint32_t status;
+  uint32_t nseeds;
+  uint32_t tiles;          // 32x8 tiles visited
+  uint32_t pad;
+  uint64_t rays_eval;      // rays evaluated (FP32 path + FP64 path)
+  uint64_t rays_fp64;      // rays evaluated in FP64
+};
+
+constexpr double kWsumScale = 4294967296.0;  // 2^32
+
+// ---------------------------------------------------------------------------
+// kernels' host launchers (seeds.cu, fill.cu)
+// ---------------------------------------------------------------------------
+void upload_trig_tables();  // Laguerre kick table + phase samples, once per device
+
+void launch_lens_setup(const LensSpec* d_specs, int nlens, DevLens* d_lenses, cx* d_cc,
+                       cx* d_ca, cudaStream_t st);
+
+void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const DevLens* d_lenses,
+                  const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
+                  cudaStream_t st);
+
+void launch_point_lc(const Traj* d_trajs, const SeedJob* d_jobs, int njobs,
+                     const DevLens* d_lenses, double* d_amp, cudaStream_t st);
+
+struct FillScratch {
+  uint64_t* keys;          // [ctas << cap_log2]
+  uint32_t* recs;          // [ctas << cap_log2][32 words]
+  uint32_t* ring;          // [ctas << cap_log2]
+  uint32_t* used;          // [ctas << cap_log2]
+  unsigned* next_point;    // work counter (1 word)
+  int ctas;
+  int cap_log2;
+  // optional export of the filled masks: records of kDumpWords words
+  // (point, tx, ty, F[8]); nullptr disables it
+  uint32_t* dump;
+  unsigned* dump_count;
+  unsigned dump_cap;
+};
+constexpr int kDumpWords = 11;
+
+size_t fill_scratch_bytes(int ctas, int cap_log2);
+void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, cudaStream_t st);
+
+enum FillMode : int { kFillFp64 = 0, kFillSplit = 1 };
+
+void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
+                 const int32_t* d_seeds, PointOut* d_out, const FillScratch& s, int mode,
+                 int threads, cudaStream_t st);
+
+int fill_default_ctas();
+
+}  // namespace tl

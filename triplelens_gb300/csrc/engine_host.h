@@ -1,0 +1,61 @@
+// engine_host.h - process-wide GPU resources of liblcirs.so: one stream, grow-only
+// device buffers and the fill kernel's per-CTA tile tables.  Calls into the
+// engine are serialised by `mu` (the reference's objects are not thread-safe
+// either; the engine is shared by every object of the process).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <mutex>
+
+#include "engine.h"
+
+namespace tl {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  void* need(size_t bytes);
+};
+
+struct Run {
+  Traj* trajs;
+  SeedJob* jobs;
+  PointIn* points;
+  int32_t* seeds;
+  PointOut* out;
+  uint32_t* dump;
+  unsigned* dump_count;
+  unsigned dump_cap;
+};
+
+class Engine {
+ public:
+  static Engine& get();
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  int last_error = 0;
+  DevBuf scratch_specs, scratch_amp;
+
+  // sizes the per-call buffers for npoints points, ntraj curves, njobs jobs
+  Run prepare(size_t npoints, size_t ntraj, size_t njobs, bool dump);
+  // runs the fill kernel over the points of R
+  void fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
+  void fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
+  bool check(cudaError_t e);
+  int fill_ctas() const { return fs_.ctas; }
+  int fill_cap_log2() const { return fs_.cap_log2; }
+  void set_fill_config(int ctas, int cap_log2, int threads);
+
+ private:
+  Engine();
+  void ensure_fill_scratch();
+  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_;
+  void* fill_base_ = nullptr;
+  size_t fill_bytes_ = 0;
+  FillScratch fs_{};
+  int want_ctas_ = 0, want_cap_log2_ = 17, threads_ = 256;
+};
+
+}  // namespace tl

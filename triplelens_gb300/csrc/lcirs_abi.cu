@@ -1,0 +1,404 @@
+// lcirs_abi.cu - LightCurveIRS class and the reference's C ABI on top of the
+// GPU engine (seeds.cu, fill.cu).
+//
+// Reference interface replaced: src/LightCurves/lcirs.cc:515-609 (extern "C"
+// block) and the LightCurveIRS class (src/LightCurves/lcirs.h:30-116).
+// Everything numeric runs on the GPU: critical curve/caustics/grid
+// (lens_setup_kernel), images and seeds (seeds_kernel), the amoeba fill
+// (fill_kernel).  The host builds descriptors, moves data and prints the
+// reference's per-point lines.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "engine_host.h"
+#include "lcirs.hpp"
+
+using tl::cx;
+
+struct LightCurveIRS::Impl {
+  tl::LensSpec spec;
+  tl::DevLens lens;         // host copy
+  tl::DevLens* d_lens = nullptr;
+  cx* d_cc = nullptr;
+  cx* d_ca = nullptr;
+  std::vector<double> lcFull;  // n+1 magnifications
+};
+
+namespace {
+
+void setup_object(LightCurveIRS* o) {
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  auto* I = o->impl;
+  I->spec = tl::make_lens_spec(o->a, o->b, o->th, o->m2, o->m3, o->sourceRadius,
+                               o->pointsPerRadius, o->ldA, o->ldB, o->intensityCoeff);
+  if (!I->d_lens) {
+    E.check(cudaMalloc(&I->d_lens, sizeof(tl::DevLens)));
+    E.check(cudaMalloc(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen));
+    E.check(cudaMalloc(&I->d_ca, sizeof(cx) * tl::kBranches * tl::kCCLen));
+  }
+  tl::LensSpec* d_spec = (tl::LensSpec*)E.scratch_specs.need(sizeof(tl::LensSpec));
+  E.check(cudaMemcpyAsync(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, E.stream));
+  tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, E.stream);
+  E.check(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost,
+                          E.stream));
+  E.check(cudaStreamSynchronize(E.stream));
+  const tl::Grid& g2 = I->lens.g;
+  o->grid[0] = g2.corner_x;
+  o->grid[1] = g2.corner_y;
+  o->grid[2] = g2.top_x;
+  o->grid[3] = g2.top_y;
+  o->grid[4] = g2.size_double;
+  o->grid[5] = g2.h;
+  o->grid[6] = g2.amp_scale;
+  o->grid[7] = (double)g2.n;
+}
+
+}  // namespace
+
+LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, double m3_,
+                             double sourceSize, unsigned int lcLength_, long ppr)
+    : a(a_), b(b_), th(th_), m1(1.0 - m2_ - m3_), m2(m2_), m3(m3_), sourceRadius(sourceSize),
+      lcLength(lcLength_), pointsPerRadius(ppr) {
+  impl = new Impl();
+  // default limb darkening A = 0.6, B = 0.4 (limbdarkeningmodel.cc:8-15)
+  ldA = 0.6;
+  ldB = 0.4;
+  intensityCoeff = 1.0 / (ldA + 2.0 / 3.0 * ldB);
+  lcVec.assign(lcLength, 0.0);
+  impl->lcFull.assign((size_t)lcLength + 1, 0.0);
+  setup_object(this);
+}
+
+LightCurveIRS::~LightCurveIRS() {
+  if (impl) {
+    cudaFree(impl->d_lens);
+    cudaFree(impl->d_cc);
+    cudaFree(impl->d_ca);
+    delete impl;
+  }
+}
+
+void LightCurveIRS::setLimbDarkening(const std::string& model, double v) {
+  if (model == "linear") {
+    // limbdarkeningmodel.cc:18-28
+    const double i0 = 1.0 / ((1.0 - v / 3.0));
+    ldA = i0 * (1.0 - v);
+    ldB = i0 * v;
+    intensityCoeff = 1.0;
+  } else {
+    ldA = 0.6;
+    ldB = 0.4;
+    intensityCoeff = 1.0 / (ldA + 2.0 / 3.0 * ldB);
+  }
+  // _ampScale = intensityCoeff/pi/ppr^2 (lcirs.cc:94-101)
+  const double ppr = (double)(int)pointsPerRadius;
+  grid[6] = intensityCoeff / 3.14159265358979323846 / (ppr * ppr);
+  impl->lens.g.amp_scale = grid[6];
+  impl->lens.ld_a = ldA;
+  impl->lens.ld_b = ldB;
+  impl->spec.ld_a = ldA;
+  impl->spec.ld_b = ldB;
+  impl->spec.intensity = intensityCoeff;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  E.check(cudaMemcpyAsync(impl->d_lens, &impl->lens, sizeof(tl::DevLens), cudaMemcpyHostToDevice,
+                          E.stream));
+  E.check(cudaStreamSynchronize(E.stream));
+}
+
+void LightCurveIRS::setAmoebaPrintOut(bool on, std::string amoebaFilename,
+                                      std::string parFilename) {
+  amoebaPrintOut_ = on;
+  amoebaFilename_ = amoebaFilename;
+  parFilename_ = parFilename;
+}
+
+// lcirs.cc:479-512 (including the reference's "m3" field written with m2)
+void LightCurveIRS::printOutLCParameters() {
+  std::ofstream f(parFilename_);
+  const char* ind = "\t";
+  f << "{" << '\n';
+  f << ind << "\"sourceRadius\": " << sourceRadius << ",\n";
+  f << ind << "\"pointsPerRadius\": " << (int)pointsPerRadius << ",\n";
+  f << ind << "\"imgPlaneSize\": " << impl->lens.g.n << ",\n";
+  f << ind << "\"imgPlaneSizeDouble\": " << impl->lens.g.size_double << ",\n";
+  f << ind << "\"bottomLeftCornerImgX\": " << impl->lens.g.corner_x << ",\n";
+  f << ind << "\"bottomLeftCornerImgY\": " << impl->lens.g.corner_y << ",\n";
+  f << ind << "\"topRightCornerImgX\": " << impl->lens.g.top_x << ",\n";
+  f << ind << "\"topRightCornerImgY\": " << impl->lens.g.top_y << ",\n";
+  f << ind << "\"a\": " << a << ",\n";
+  f << ind << "\"b\": " << b << ",\n";
+  f << ind << "\"th\": " << th << ",\n";
+  f << ind << "\"m1\": " << m1 << ",\n";
+  f << ind << "\"m2\": " << m2 << ",\n";
+  f << ind << "\"m3\": " << m2 << ",\n";
+  f << ind << "\"z1x\": " << 0.0 << ",\n";
+  f << ind << "\"z1y\": " << 0.0 << ",\n";
+  f << ind << "\"z2x\": " << impl->lens.L.z2.re << ",\n";
+  f << ind << "\"z2y\": " << impl->lens.L.z2.im << ",\n";
+  f << ind << "\"z3x\": " << impl->lens.L.z3.re << ",\n";
+  f << ind << "\"z3y\": " << impl->lens.L.z3.im << "\n";
+  f << "}";
+}
+
+void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
+                            const int32_t* extSeeds, const int32_t* extN) {
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  const uint32_t n = lcLength;
+  const size_t np = (size_t)n + 1;
+  tl::Traj T;
+  T.x0 = s.real();
+  T.y0 = s.imag();
+  T.x1 = e.real();
+  T.y1 = e.imag();
+  T.n = n;
+  T.lens = 0;
+  T.point_base = 0;
+  std::vector<tl::SeedJob> jobs;
+  for (uint32_t f = 0; f < np; f += tl::kChainChunk) {
+    tl::SeedJob j;
+    j.traj = 0;
+    j.first = (int32_t)f;
+    j.count = (int32_t)std::min<size_t>(tl::kChainChunk, np - f);
+    j.pad = 0;
+    jobs.push_back(j);
+  }
+  tl::Run R = E.prepare(np, 1, jobs.size(), amoebaPrintOut_);
+  E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
+  E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                          cudaMemcpyHostToDevice, E.stream));
+  tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, impl->d_lens, impl->d_ca, R.points, R.seeds,
+                   R.out, E.stream);
+  if (extSeeds) {
+    // replace the seeds with the caller's, keep the positions
+    std::vector<tl::PointOut> hout(np);
+    E.check(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
+                            E.stream));
+    E.check(cudaStreamSynchronize(E.stream));
+    for (size_t i = 0; i < np; i++) {
+      hout[i].nseeds = (uint32_t)std::min(extN[i], tl::kMaxSeeds);
+      hout[i].status = 0;
+    }
+    E.check(cudaMemcpyAsync(R.out, hout.data(), sizeof(tl::PointOut) * np, cudaMemcpyHostToDevice,
+                            E.stream));
+    E.check(cudaMemcpyAsync(R.seeds, extSeeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
+                            cudaMemcpyHostToDevice, E.stream));
+  }
+  E.fill(R, np, impl->d_lens, precision);
+  std::vector<tl::PointOut> hout(np);
+  E.check(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
+                          E.stream));
+  seeds.resize(np * 2 * tl::kMaxSeeds);
+  nseeds.resize(np);
+  E.check(cudaMemcpyAsync(seeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
+                          cudaMemcpyDeviceToHost, E.stream));
+  std::vector<uint32_t> dump;
+  unsigned ndump = 0;
+  if (amoebaPrintOut_) {
+    E.check(cudaMemcpyAsync(&ndump, R.dump_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            E.stream));
+  }
+  E.check(cudaStreamSynchronize(E.stream));
+  if (amoebaPrintOut_) {
+    if (ndump > R.dump_cap) {
+      std::cout << "amoeba dump truncated: " << ndump << " tiles, capacity " << R.dump_cap << "\n";
+      ndump = R.dump_cap;
+    }
+    dump.resize((size_t)ndump * tl::kDumpWords);
+    E.check(cudaMemcpy(dump.data(), R.dump, sizeof(uint32_t) * dump.size(),
+                       cudaMemcpyDeviceToHost));
+  }
+  counts.resize(np);
+  status.resize(np);
+  lastStatus = E.last_error ? 0x100u : 0u;
+  stats[0] = stats[1] = stats[2] = 0;
+  const double scale = impl->lens.g.amp_scale;
+  for (size_t i = 0; i < np; i++) {
+    counts[i] = hout[i].count;
+    status[i] = hout[i].status;
+    nseeds[i] = (int32_t)hout[i].nseeds;
+    lastStatus |= hout[i].status;
+    stats[0] += hout[i].rays_eval;
+    stats[1] += hout[i].rays_fp64;
+    stats[2] += hout[i].tiles;
+    const double wsum = (double)hout[i].wsum_fx / tl::kWsumScale;
+    impl->lcFull[i] = wsum * scale;
+  }
+  for (size_t i = 0; i < n; i++) lcVec[i] = impl->lcFull[i];
+  if (verbose) {
+    std::cout << "IRS called with imgPlaneSize:" << impl->lens.g.n << "\n";
+    for (size_t i = 0; i < np; i++) {
+      const double t = double(i) / double(n);
+      const double px = s.real() + (e.real() - s.real()) * t;
+      const double py = s.imag() + (e.imag() - s.imag()) * t;
+      std::cout << "started pos:" << i << ", (" << px << "," << py << ")\n";
+      std::cout << "irs amplification: " << impl->lcFull[i] << " and the count " << counts[i]
+                << " and amp scale " << scale << "\n";
+    }
+  }
+  if (amoebaPrintOut_) {
+    // rows of every point from its tile masks: maximal runs, merged across
+    // neighbouring tiles (amoeba.cc:90-108 writes "ny,xleft,xright")
+    std::vector<std::vector<std::pair<int64_t, std::pair<int64_t, int64_t>>>> per(np);
+    for (unsigned d = 0; d < ndump; d++) {
+      const uint32_t* r = &dump[(size_t)d * tl::kDumpWords];
+      const uint32_t p = r[0];
+      if (p >= np) continue;
+      const int64_t tx = r[1], ty = r[2];
+      for (int row = 0; row < 8; row++) {
+        uint32_t m = r[3 + row];
+        while (m) {
+          const int lo = __builtin_ctz(m);
+          const uint32_t sh = m >> lo;
+          const int len = (~sh == 0u) ? 32 - lo : __builtin_ctz(~sh);
+          per[p].push_back({ty * 8 + row, {tx * 32 + lo, tx * 32 + lo + len - 1}});
+          m &= (len + lo >= 32) ? 0u : ~((1u << (lo + len)) - 1u);
+        }
+      }
+    }
+    for (size_t i = 0; i < np; i++) {
+      auto& v = per[i];
+      std::sort(v.begin(), v.end());
+      std::ofstream f(amoebaFilename_ + std::to_string(i));
+      for (size_t k = 0; k < v.size();) {
+        const int64_t ny = v[k].first;
+        int64_t xl = v[k].second.first, xr = v[k].second.second;
+        size_t q = k + 1;
+        while (q < v.size() && v[q].first == ny && v[q].second.first == xr + 1) {
+          xr = v[q].second.second;
+          q++;
+        }
+        f << ny << "," << xl << "," << xr << "\n";
+        k = q;
+      }
+    }
+  }
+}
+
+void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
+  if (amoebaPrintOut_) printOutLCParameters();
+  runFill(s, e, nullptr, nullptr);
+}
+
+void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  const uint32_t n = lcLength;
+  if (n == 0) return;
+  tl::Traj T;
+  T.x0 = s.real();
+  T.y0 = s.imag();
+  T.x1 = e.real();
+  T.y1 = e.imag();
+  T.n = n;
+  T.lens = 0;
+  T.point_base = 0;
+  std::vector<tl::SeedJob> jobs;
+  for (uint32_t f = 0; f < n; f += tl::kChainChunk) {
+    tl::SeedJob j;
+    j.traj = 0;
+    j.first = (int32_t)f;
+    j.count = (int32_t)std::min<uint32_t>(tl::kChainChunk, n - f);
+    j.pad = 0;
+    jobs.push_back(j);
+  }
+  tl::Run R = E.prepare(n, 1, jobs.size(), false);
+  E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
+  E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                          cudaMemcpyHostToDevice, E.stream));
+  double* d_amp = (double*)E.scratch_amp.need(sizeof(double) * n);
+  tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, E.stream);
+  E.check(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                          E.stream));
+  E.check(cudaStreamSynchronize(E.stream));
+  for (size_t i = 0; i < n; i++) impl->lcFull[i] = lcVec[i];
+}
+
+// ---------------------------------------------------------------------------
+// C ABI (src/LightCurves/lcirs.cc:515-609 and additive entry points)
+// ---------------------------------------------------------------------------
+extern "C" {
+
+LightCurveIRS* lcirs_new(double a, double b, double th, double m2, double m3, double sourceSize,
+                         unsigned int lcLength, long pointsPerRadius) {
+  return new LightCurveIRS(a, b, th, m2, m3, sourceSize, lcLength, pointsPerRadius);
+}
+
+void get_lc(LightCurveIRS* lc, double iniX, double iniY, double finX, double finY) {
+  lc->getLC({iniX, iniY}, {finX, finY});
+}
+
+void get_lc_irs(LightCurveIRS* lc, double iniX, double iniY, double finX, double finY) {
+  lc->getLCIRS({iniX, iniY}, {finX, finY});
+}
+
+void copy_lc(LightCurveIRS* lc, double* out) {
+  const size_t n = lc->lcVec.size();
+  for (size_t i = 0; i < n; i++) out[i] = lc->lcVec[i];
+}
+
+void set_limb_darkening(LightCurveIRS* lc, const char* model, double v) {
+  if (strcmp(model, "linear") == 0) {
+    std::cout << "model is linear\n";
+    lc->setLimbDarkening("linear", v);
+  } else {
+    std::cout << "model is default\n";
+    lc->setLimbDarkening("default", v);
+  }
+}
+
+void set_amoeba_printout(LightCurveIRS* lc, const char* amoebaFilename, const char* parFilename) {
+  lc->setAmoebaPrintOut(true, std::string(amoebaFilename), std::string(parFilename));
+}
+
+void lcirs_delete(LightCurveIRS* lc) { delete lc; }
+
+unsigned int lcirs_last_status(LightCurveIRS* lc) { return lc->lastStatus; }
+
+void lcirs_copy_counts(LightCurveIRS* lc, uint64_t* out) {
+  for (size_t i = 0; i < lc->counts.size(); i++) out[i] = lc->counts[i];
+}
+
+void lcirs_copy_lc_full(LightCurveIRS* lc, double* out) {
+  for (size_t i = 0; i <= lc->lcLength; i++) out[i] = lc->impl->lcFull[i];
+}
+
+void lcirs_copy_status(LightCurveIRS* lc, uint32_t* out) {
+  for (size_t i = 0; i < lc->status.size(); i++) out[i] = lc->status[i];
+}
+
+void lcirs_set_verbose(LightCurveIRS* lc, int v) { lc->verbose = v; }
+
+void lcirs_grid(LightCurveIRS* lc, double* out8) {
+  for (int k = 0; k < 8; k++) out8[k] = lc->grid[k];
+}
+
+void lcirs_copy_seeds(LightCurveIRS* lc, int32_t* seeds, int32_t* nseeds) {
+  for (size_t i = 0; i < lc->seeds.size(); i++) seeds[i] = lc->seeds[i];
+  for (size_t i = 0; i < lc->nseeds.size(); i++) nseeds[i] = lc->nseeds[i];
+}
+
+void lcirs_fill_from_seeds(LightCurveIRS* lc, double iniX, double iniY, double finX, double finY,
+                           const int32_t* seeds, const int32_t* nseeds) {
+  lc->runFill({iniX, iniY}, {finX, finY}, seeds, nseeds);
+}
+
+void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3) {
+  for (int k = 0; k < 3; k++) out3[k] = lc->stats[k];
+}
+
+void lcirs_set_precision(LightCurveIRS* lc, int mode) { lc->precision = mode; }
+
+}  // extern "C"
