@@ -99,6 +99,11 @@ void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3);
  * tile-relative map with an FP64 guard band at the limb (default). */
 void lcirs_set_precision(LightCurveIRS* lc, int mode);
 
+/* Fill-kernel diagnostics of the last get_lc_irs, n+1 entries: bits 0-15
+ * the largest number of passes over one tile, bit 16 pass limit reached,
+ * bit 17 dequeue limit reached, bits 24-31 the tile state seen then. */
+void lcirs_copy_diag(LightCurveIRS* lc, uint32_t* diag);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,7 @@ struct LightCurveIRS {
   std::vector<double> lcVec;          // n entries visible (copy_lc), n+1 stored
   std::vector<uint64_t> counts;       // rays per point of the last IRS curve
   std::vector<uint32_t> status;       // status bits per point
+  std::vector<uint32_t> diag;         // fill-kernel diagnostics per point
   std::vector<int32_t> seeds;         // (n+1) x 64 x 2
   std::vector<int32_t> nseeds;        // n+1
   uint64_t stats[3] = {0, 0, 0};      // rays evaluated, FP64 rays, tiles

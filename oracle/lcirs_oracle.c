@@ -186,6 +186,8 @@ struct orc_lcirs {
   int have_temp;
   int chain_chunk; /* 0: one warm-start chain (reference); K: restart every K points */
   int fragile;     /* set when an image decision sat near the filter radius */
+  double fragile_band; /* residual below which a filter/lens-equation
+                          disagreement marks the point fragile */
   /* amoeba (amoeba.h) */
   orc_row *rows;
   long rows_cap, rows_used;
@@ -394,14 +396,44 @@ static double img_residual(const orc_lcirs *o, cx img, cx src) {
   return cabs_(csub(t, src));
 }
 
+/* Is the root a genuine solution of the lens equation?  Newton's method on
+ * F(z) = z - sum m_i/conj(z - z_i) - zeta, whose linearisation is
+ * F(z+d) = F + d + gamma conj(d) with gamma = sum m_i/conj(z - z_i)^2, so
+ * d = (gamma conj(F) - F)/(1 - |gamma|^2).  Diagnostic only: it never changes
+ * the image set, it tells whether the filter's decision was safe. */
+static int true_image(const orc_lcirs *o, cx z, cx zeta) {
+  const cx zs[3] = {o->z1, o->z2, o->z3};
+  const double ms[3] = {o->m1, o->m2, o->m3};
+  cx z0 = z;
+  for (int it = 0; it < 30; it++) {
+    cx F = csub(z, zeta), g = mk(0.0, 0.0);
+    for (int i = 0; i < 3; i++) {
+      cx w = cconj(csub(z, zs[i]));
+      F = csub(F, rdiv(ms[i], w));
+      g = cadd(g, rdiv(ms[i], cmul(w, w)));
+    }
+    double det = 1.0 - cnorm(g);
+    if (cabs_(F) < 1e-13) return cabs_(csub(z, z0)) < 1e-3;
+    if (fabs(det) < 1e-300) return 0;
+    cx d = cscale(csub(cmul(g, cconj(F)), F), 1.0 / det);
+    z = cadd(z, d);
+  }
+  return 0;
+}
+
 static int filter_images(orc_lcirs *o, const cx *roots, cx zeta, cx *imgs) {
   int n = 0;
   for (int k = 0; k < 10; k++) {
-    if (img_check(o, roots[k], zeta, 1.0e-6)) imgs[n++] = roots[k];
-    /* a residual within a decade of the 1e-6 filter radius makes the image
-     * set depend on rounding (double roots at caustic points) */
+    int accepted = img_check(o, roots[k], zeta, 1.0e-6);
+    if (accepted) imgs[n++] = roots[k];
+    /* The image set depends on rounding when a residual sits within a decade
+     * of the 1e-6 filter radius (double roots at caustic points), or when
+     * the filter's verdict disagrees with the lens equation itself (roots
+     * next to a small-mass lens, where the residual amplifies the root's
+     * rounding error by m_i/|z - z_i|^2). */
     double r = img_residual(o, roots[k], zeta);
     if (r > 1.0e-7 && r < 1.0e-5) o->fragile = 1;
+    if (r < o->fragile_band && accepted != true_image(o, roots[k], zeta)) o->fragile = 1;
   }
   return n;
 }
@@ -758,6 +790,7 @@ orc_lcirs *orc_new(double a, double b, double th, double m2, double m3,
   o->z2 = mk(a, 0.0);
   o->z3 = mk(b * cos(th), b * sin(th));
   o->is_binary_img = (a == 0.0 || b == 0.0 || m3 == 0.0);
+  o->fragile_band = 1.0e-4;
   o->rho = rho;
   o->rho2 = rho * rho;
   o->lc_length = lc_length;
@@ -817,6 +850,7 @@ static inline void chain_restart(orc_lcirs *o, unsigned i) {
 }
 
 void orc_set_chain_chunk(orc_lcirs *o, int k) { o->chain_chunk = k; }
+void orc_set_fragile_band(orc_lcirs *o, double r) { o->fragile_band = r; }
 
 static inline cx traj_pos(cx s, cx e, unsigned i, unsigned n) {
   double t = (double)i / (double)n;

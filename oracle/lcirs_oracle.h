@@ -39,6 +39,10 @@ void orc_free(orc_lcirs *o);
 /* Restart the image solver's warm-start chain cold every k points
  * (k = 0: a single chain, as the reference). */
 void orc_set_chain_chunk(orc_lcirs *o, int k);
+/* Residual below which a root rejected by the 1e-6 filter although it solves
+ * the lens equation (or accepted although it does not) marks its point as
+ * fragile (default 1e-4). */
+void orc_set_fragile_band(orc_lcirs *o, double r);
 
 /* lcirs.cc:579-598 (set_limb_darkening): model "linear" -> v-normalised. */
 void orc_set_limb_darkening(orc_lcirs *o, const char *model, double v);

@@ -43,6 +43,7 @@ def lib():
         L.orc_get_lc_irs.argtypes = [vp, d, d, d, d, dp, i64p]
         L.orc_lc_seeds.argtypes = [vp, d, d, d, d, ctypes.c_int, i64p, vp, vp]
         L.orc_set_chain_chunk.argtypes = [vp, ctypes.c_int]
+        L.orc_set_fragile_band.argtypes = [vp, d]
         L.orc_lc_seeds.restype = ctypes.c_long
         L.orc_fill.argtypes = [vp, d, d, i64p, ctypes.c_int, dp, i64p]
         L.orc_last_amoeba.argtypes = [vp, i64p, ctypes.c_long]
@@ -113,6 +114,9 @@ class OracleIRS:
     def set_chain_chunk(self, k):
         """Restart the warm-start chain every k points (0: one chain)."""
         self.L.orc_set_chain_chunk(self.obj, int(k))
+
+    def set_fragile_band(self, r):
+        self.L.orc_set_fragile_band(self.obj, float(r))
 
     def lc_seeds(self, x0, y0, x1, y1, max_seeds=64):
         """Seed pixels per point, their number, and the fragile flags."""

@@ -10,6 +10,12 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # TL_WATCHDOG=<seconds>: dump every thread's Python stack periodically
+    # (shows which library call a slow test is in, even inside C code)
+    w = os.environ.get("TL_WATCHDOG")
+    if w:
+        import faulthandler
+        faulthandler.dump_traceback_later(float(w), repeat=True)
 
 
 @pytest.fixture(scope="session")

@@ -152,14 +152,18 @@ def main():
     for k in range(len(lenses)):
         c, a = run_curve(REF_LIBS["nfc"], lenses[k], trajs[k], 200)
         c2["counts_%d" % k], c2["amps_%d" % k] = c, a
+        # the default-flag build (FMA contraction on): the reference's own
+        # build-to-build spread on these curves
+        c2["counts_fast_%d" % k], _ = run_curve(REF_LIBS["fast"], lenses[k], trajs[k], 200)
     np.savez_compressed(os.path.join(HERE, "config2_short.npz"), **c2)
     print("wrote config2_short.npz")
 
     if args.c2:
         lenses, trajs, n = workloads.config2(seed=0, n_curves=1)
         c, a = run_curve(REF_LIBS["nfc"], lenses[0], trajs[0], n)
+        cf, _ = run_curve(REF_LIBS["fast"], lenses[0], trajs[0], n)
         np.savez_compressed(os.path.join(HERE, "config2_seed0.npz"), lenses=lenses, trajs=trajs,
-                            n=n, counts=c, amps=a)
+                            n=n, counts=c, amps=a, counts_fast=cf)
         print("wrote config2_seed0.npz")
 
 

@@ -117,6 +117,9 @@ def test_config1_amoeba_sets_match_reference(oracle_lib, golden_c1):
 
 
 def test_config2_short_counts_match_reference(oracle_lib):
+    """Config-2 lenses (small planets): the oracle equals the reference on
+    every point whose image decisions are not rounding-dependent, except
+    where the reference's two builds disagree with each other."""
     import os
     z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_short.npz"))
     n = int(z["n"])
@@ -126,12 +129,23 @@ def test_config2_short_counts_match_reference(oracle_lib):
         o = oracle_lib.OracleIRS(*L[:5], L[5], n, int(L[7]))
         o.set_limb_darkening("linear", L[6])
         seeds, cnt, fragile = o.lc_seeds(*t)
-        ref = z["counts_%d" % k]
-        # fill a spread of points (whole curve would take ~10 s per curve)
-        for p in range(0, n + 1, 20):
-            if fragile[p]:
+        ref, ref_fast = z["counts_%d" % k], z["counts_fast_%d" % k]
+        # fill a spread of points (the whole curve would take ~10 s per curve)
+        for p in range(0, n + 1, 10):
+            if fragile[p] or ref[p] != ref_fast[p]:
                 continue
             x = t[0] + (t[2] - t[0]) * (p / n)
             y = t[1] + (t[3] - t[1]) * (p / n)
             _, c = o.fill(x, y, seeds[p, :cnt[p]])
             assert c == ref[p], (k, p)
+
+
+def test_reference_build_spread_is_small():
+    """The reference's own builds (FMA contraction off/on) differ by a few
+    rays on points with tiny images next to small-mass lenses."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_short.npz"))
+    for k in range(len(z["lenses"])):
+        a = z["counts_%d" % k].astype(np.int64)
+        b = z["counts_fast_%d" % k].astype(np.int64)
+        assert np.max(np.abs(a - b)) <= 64

@@ -84,7 +84,8 @@ struct PointOut {
   uint32_t status;
   uint32_t nseeds;
   uint32_t tiles;          // 32x8 tiles visited
-  uint32_t pad;
+  uint32_t diag;           // bits 0-15: max passes over one tile; 16: pass
+                           // limit hit; 17: dequeue limit hit; 24-31: state
   uint64_t rays_eval;      // rays evaluated (FP32 path + FP64 path)
   uint64_t rays_fp64;      // rays evaluated in FP64
 };
@@ -111,6 +112,10 @@ struct FillScratch {
   uint32_t* recs;          // [ctas << cap_log2][32 words]
   uint32_t* ring;          // [ctas << cap_log2]
   uint32_t* used;          // [ctas << cap_log2]
+  // super-tile expansion table (split-precision ray map), per CTA
+  uint64_t* skeys;         // [ctas << kSuperLog2]
+  uint32_t* sents;         // [ctas << kSuperLog2][32 words]
+  uint32_t* sused;         // [ctas << kSuperLog2]
   unsigned* next_point;    // work counter (1 word)
   int ctas;
   int cap_log2;
@@ -121,6 +126,7 @@ struct FillScratch {
   unsigned dump_cap;
 };
 constexpr int kDumpWords = 11;
+constexpr int kSuperLog2 = 12;   // super-tile table capacity per CTA (entries)
 
 size_t fill_scratch_bytes(int ctas, int cap_log2);
 void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, cudaStream_t st);

@@ -1,6 +1,7 @@
 // engine_host.cu - process-wide GPU resources of the engine (see engine_host.h).
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 
@@ -39,7 +40,19 @@ Engine::Engine() {
   check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   upload_trig_tables();
   if (const char* c = getenv("TL_FILL_CAP_LOG2")) want_cap_log2_ = atoi(c);
+  if (const char* c = getenv("TL_TRACE")) {
+    tracing = atoi(c) != 0;
+    sync_steps = atoi(c) >= 2;
+  }
   if (const char* c = getenv("TL_FILL_CTAS")) want_ctas_ = atoi(c);
+}
+
+void Engine::trace(const char* what) {
+  if (!tracing) return;
+  static const auto t0 = std::chrono::steady_clock::now();
+  const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  fprintf(stderr, "[tl %10.4f] %s\n", t, what);
+  fflush(stderr);
 }
 
 bool Engine::check(cudaError_t e) {

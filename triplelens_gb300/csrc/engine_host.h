@@ -44,6 +44,10 @@ class Engine {
   void fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
   void fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
   bool check(cudaError_t e);
+  // TL_TRACE=1: print every host step with a timestamp to stderr
+  void trace(const char* what);
+  bool tracing = false;
+  bool sync_steps = false;  // TL_TRACE=2: also synchronise after every launch
   int fill_ctas() const { return fs_.ctas; }
   int fill_cap_log2() const { return fs_.cap_log2; }
   void set_fill_config(int ctas, int cap_log2, int threads);

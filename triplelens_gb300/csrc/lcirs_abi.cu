@@ -39,6 +39,7 @@ namespace {
 void setup_object(LightCurveIRS* o) {
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
+  E.trace("setup_object: lens set-up");
   auto* I = o->impl;
   I->spec = tl::make_lens_spec(o->a, o->b, o->th, o->m2, o->m3, o->sourceRadius,
                                o->pointsPerRadius, o->ldA, o->ldB, o->intensityCoeff);
@@ -53,6 +54,7 @@ void setup_object(LightCurveIRS* o) {
   E.check(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost,
                           E.stream));
   E.check(cudaStreamSynchronize(E.stream));
+  E.trace("setup_object: done");
   const tl::Grid& g2 = I->lens.g;
   o->grid[0] = g2.corner_x;
   o->grid[1] = g2.corner_y;
@@ -81,6 +83,7 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
 }
 
 LightCurveIRS::~LightCurveIRS() {
+  tl::Engine::get().trace("delete object");
   if (impl) {
     cudaFree(impl->d_lens);
     cudaFree(impl->d_cc);
@@ -90,6 +93,7 @@ LightCurveIRS::~LightCurveIRS() {
 }
 
 void LightCurveIRS::setLimbDarkening(const std::string& model, double v) {
+  tl::Engine::get().trace("setLimbDarkening");
   if (model == "linear") {
     // limbdarkeningmodel.cc:18-28
     const double i0 = 1.0 / ((1.0 - v / 3.0));
@@ -175,6 +179,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
     j.pad = 0;
     jobs.push_back(j);
   }
+  E.trace("runFill: prepare");
   tl::Run R = E.prepare(np, 1, jobs.size(), amoebaPrintOut_);
   E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
   E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
@@ -196,7 +201,17 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
     E.check(cudaMemcpyAsync(R.seeds, extSeeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
                             cudaMemcpyHostToDevice, E.stream));
   }
+  E.trace("runFill: seeds launched");
+  if (E.sync_steps) {
+    E.check(cudaStreamSynchronize(E.stream));
+    E.trace("runFill: seeds done");
+  }
   E.fill(R, np, impl->d_lens, precision);
+  E.trace("runFill: fill launched");
+  if (E.sync_steps) {
+    E.check(cudaStreamSynchronize(E.stream));
+    E.trace("runFill: fill done");
+  }
   std::vector<tl::PointOut> hout(np);
   E.check(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
                           E.stream));
@@ -220,14 +235,17 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
     E.check(cudaMemcpy(dump.data(), R.dump, sizeof(uint32_t) * dump.size(),
                        cudaMemcpyDeviceToHost));
   }
+  E.trace("runFill: results copied");
   counts.resize(np);
   status.resize(np);
+  diag.resize(np);
   lastStatus = E.last_error ? 0x100u : 0u;
   stats[0] = stats[1] = stats[2] = 0;
   const double scale = impl->lens.g.amp_scale;
   for (size_t i = 0; i < np; i++) {
     counts[i] = hout[i].count;
     status[i] = hout[i].status;
+    diag[i] = hout[i].diag;
     nseeds[i] = (int32_t)hout[i].nseeds;
     lastStatus |= hout[i].status;
     stats[0] += hout[i].rays_eval;
@@ -400,5 +418,9 @@ void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3) {
 }
 
 void lcirs_set_precision(LightCurveIRS* lc, int mode) { lc->precision = mode; }
+
+void lcirs_copy_diag(LightCurveIRS* lc, uint32_t* out) {
+  for (size_t i = 0; i < lc->diag.size(); i++) out[i] = lc->diag[i];
+}
 
 }  // extern "C"

@@ -289,7 +289,7 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
       o.status = status;
       o.nseeds = nseed < (uint32_t)kMaxSeeds ? nseed : (uint32_t)kMaxSeeds;
       o.tiles = 0;
-      o.pad = 0;
+      o.diag = 0;
       o.rays_eval = 0;
       o.rays_fp64 = 0;
       out[p] = o;

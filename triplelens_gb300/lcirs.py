@@ -50,6 +50,7 @@ def load_lcirs(path=None):
                                         ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]
     L.lcirs_copy_stats.argtypes = [vp, ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
     L.lcirs_set_precision.argtypes = [vp, ctypes.c_int]
+    L.lcirs_copy_diag.argtypes = [vp, ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")]
     _libs[path] = L
     return L
 
@@ -133,6 +134,11 @@ class LC_irs(object):
         s = np.ascontiguousarray(seeds, np.int32).reshape(-1)
         n = np.ascontiguousarray(nseeds, np.int32)
         self.lib_lc.lcirs_fill_from_seeds(self.obj, iniX, iniY, finX, finY, s, n)
+
+    def diag(self):
+        out = np.zeros(self.lc_len + 1, np.uint32)
+        self.lib_lc.lcirs_copy_diag(self.obj, out)
+        return out
 
     def stats(self):
         out = np.zeros(3, np.uint64)
