@@ -1,0 +1,379 @@
+"""Benchmark: finite-source light-curve points/s on one GB300 (plain GPU IRS).
+
+Workload (the configuration the metric is quoted on): random triple lenses
+from a seed, masses from ratios log-uniform in [1e-3, 1], separations
+log-uniform in [0.5, 2], trajectories of 4 theta_E with impact parameter
+uniform in [-0.5, 0.5], 5000 points each (5001 computed, the reference's
+sampling), rho = 1e-3, 500 rays per source radius, linear limb darkening
+v = 0.5.  A step = one batch of --curves light curves through the seeds
+kernel and the persistent fill kernel.  Synthetic, seeded data.
+
+JSON keys: value = points/s with inputs resident in HBM (device-timed with
+CUDA events on the launching stream, L2 flushed between steps); e2e = the same
+metric through the reference's C ABI (lcirs_new / get_lc_irs / copy_lc, host
+buffers, copies inside the timed region); roofline = the fill kernel against
+the FP32 pipe; cpu_baseline = the oracle (C restatement of the reference's
+CPU IRS) on the host's cores over a bounded sample of the same points.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "finite-source light-curve points/s at <=1e-3 rel. error: IRS vs surrogate-gated"
+UNIT = "points/s"
+FLOP_PER_RAY = 32.0       # triple map + disc test per evaluated ray
+FLOP_PER_WEIGHT = 6.0     # limb-darkened weight per accepted ray
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle over a bounded sample of points
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    lens, traj, n, idx = args
+    from oracle import oracle
+    o = oracle.OracleIRS(*lens[:5], lens[5], n, int(lens[7]))
+    o.set_limb_darkening("linear", lens[6])
+    seeds, cnt, _ = o.lc_seeds(*traj)
+    t0 = time.perf_counter()
+    rays = 0
+    for p in idx:
+        x = traj[0] + (traj[2] - traj[0]) * (p / n)
+        y = traj[1] + (traj[3] - traj[1]) * (p / n)
+        _, c = o.fill(x, y, seeds[p, :cnt[p]])
+        rays += c
+    return time.perf_counter() - t0, len(idx), rays
+
+
+def cpu_baseline(pool, procs, lenses, trajs, n, sample_points):
+    """Times the oracle's fill on `sample_points` points spread over the
+    curves, split over `procs` processes; returns (points/s all cores,
+    points/s one core, rays/s all cores, description)."""
+    ncurves = len(lenses)
+    per_curve = max(1, sample_points // ncurves)
+    tasks = []
+    for k in range(ncurves):
+        pts = np.linspace(0, n, per_curve, dtype=np.int64)
+        for chunk in np.array_split(pts, max(1, procs // ncurves)):
+            if len(chunk):
+                tasks.append((lenses[k], trajs[k], n, chunk.tolist()))
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_worker, tasks)
+    wall = time.perf_counter() - t0
+    busy = sum(r[0] for r in res)
+    npts = sum(r[1] for r in res)
+    rays = sum(r[2] for r in res)
+    desc = "%d points spread over %d curves, oracle fill from oracle seeds, %d processes" % (
+        npts, ncurves, procs)
+    return npts / wall, npts / busy, rays / wall, desc, busy
+
+
+class quiet_stdout:
+    """Sends fd 1 to /dev/null: the reference ABI reports on stdout ("model
+    is linear", per-point lines), and this script prints one JSON line."""
+
+    def __enter__(self):
+        import ctypes
+        self.libc = ctypes.CDLL(None)
+        sys.stdout.flush()
+        self.libc.fflush(None)
+        self.saved = os.dup(1)
+        nul = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(nul, 1)
+        os.close(nul)
+        return self
+
+    def __exit__(self, *a):
+        self.libc.fflush(None)
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv",
+                                          "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self, gpu_index=0):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            lines = open(self.path).read().strip().splitlines()[1:]
+        except Exception:
+            return out
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or f[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(f[1].split()[0]))
+                mx = float(f[2].split()[0])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if sm:
+            busy = [s for s in sm if s > 0.5 * max(sm)]
+            out["sm_mhz"] = float(np.median(busy))
+            out["sm_max_mhz"] = mx
+            out["reasons"] = sorted(reasons)
+            out["samples"] = len(sm)
+        return out
+
+
+def fp32_peak_tflops(sm_max_mhz):
+    """FP32 FMA peak: 152 SMs x 128 lanes x 2 flop at the SM clock."""
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        sms = 152
+    return 2.0 * 128 * sms * sm_max_mhz * 1e6 / 1e12, sms
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--curves", type=int, default=8, help="light curves per step per GPU")
+    ap.add_argument("--points", type=int, default=5000)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-sample", type=int, default=512, help="points timed on the CPU")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from triplelens_gb300 import workloads
+    # weak scaling: every rank its own curves
+    lenses, trajs, n = workloads.config2(args.seed + 1000 * rank, n_curves=args.curves,
+                                        n_points=args.points)
+    config = {"workload": "config2: %d random triple lenses x %d-point curves, rho=1e-3, "
+                          "500 rays/radius, linear LD v=0.5" % (args.curves, n),
+              "curves_per_gpu": args.curves, "points_per_curve": n + 1, "rho": 1e-3,
+              "rays_per_radius": 500, "ld_v": 0.5, "seed": args.seed,
+              "l2": "flushed between steps (256 MiB write)",
+              "parallelism": "curves sharded over %d GPU(s)" % world}
+    ncpu = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import multiprocessing as mp
+        pool = mp.get_context("spawn").Pool(ncpu)
+        vals = []
+        total_busy = 0.0
+        for step in range(args.warmup + args.steps):
+            pts_s, pts_s1, rays_s, desc, busy = cpu_baseline(
+                pool, ncpu, lenses, trajs, n, max(ncpu, args.cpu_sample // 4))
+            if step >= args.warmup:
+                vals.append(pts_s)
+                total_busy += busy
+        pool.close()
+        v = float(np.mean(vals))
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config, "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": ncpu, "kind": "port",
+                                 "sample": desc + " per step"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "note": "the reference's own CPU IRS cannot be built on this host (its sources "
+                        "are not present); its C restatement (oracle/) is timed instead"}
+        print(json.dumps(line))
+        return
+
+    # CPU pool before any GPU work (spawned workers)
+    pool = None
+    if rank == 0 and not args.no_cpu:
+        import multiprocessing as mp
+        pool = mp.get_context("spawn").Pool(ncpu)
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from triplelens_gb300.batch import Batch
+    from triplelens_gb300.lcirs import LC_irs
+
+    b = Batch()
+    b.set_lenses(lenses)
+    npts = b.set_trajectories(trajs, np.arange(len(trajs)), np.full(len(trajs), n))
+    # a dedicated stream: the library launches on it and the events are
+    # recorded on it (the legacy default stream does not order against the
+    # library's non-blocking stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_device():
+        b.run_device(1, sptr)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e1.record(stream)
+        b.run_device(2, sptr)
+        return e1
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    amp, cnt, st = b.download(sptr)
+    stats = b.stats()
+
+    tot_ms = 0.0
+    fill_ms = 0.0
+    clock_path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                              else "_work", "bench_clocks_r%d.csv" % rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(clock_path) as clk:
+        time.sleep(0.3)
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e2 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            e1 = step_device()
+            e2.record(stream)
+            e2.synchronize()
+            tot_ms += e0.elapsed_time(e2)
+            fill_ms += e1.elapsed_time(e2)
+        time.sleep(0.3)
+    torch.cuda.synchronize()
+    if dist:
+        t = torch.tensor([tot_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+        dist.barrier()
+    ms_step = tot_ms / args.steps
+    value = npts * world / (ms_step / 1e3)
+
+    # e2e: the reference-facing C ABI with host buffers, curve by curve
+    e2e_steps = max(1, min(args.steps, 3))
+    lc_objs = []
+    t_e2e = 0.0
+    h2d = d2h = 0
+    quiet = quiet_stdout().__enter__()
+    for it in range(e2e_steps + 1):
+        t0 = time.perf_counter()
+        for k in range(len(lenses)):
+            L = lenses[k]
+            lc = LC_irs(*L[:5], L[5], n, int(L[7]))
+            lc.set_verbose(0)
+            lc.set_limb_darkening("linear", L[6])
+            lc.get_lc_irs(*trajs[k])
+            out = np.zeros(n)
+            lc.copy_lc(out)
+            del lc
+        torch.cuda.synchronize()
+        if it > 0:  # first pass is a warm-up
+            t_e2e += time.perf_counter() - t0
+    quiet.__exit__()
+    # bytes across the host boundary per step (per curve: lens + trajectory
+    # parameters in, per-point results out)
+    h2d = len(lenses) * (8 * 8 + 4 * 8)
+    d2h = len(lenses) * (n + 1) * 48
+    e2e_value = npts * world / (t_e2e / e2e_steps)
+
+    peaks = measured_peaks()
+    clocks = clk.summary(local_rank)
+    sm_max = peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    peak_tf, sms = fp32_peak_tflops(sm_max)
+    fill_s = fill_ms / args.steps / 1e3
+    flops = FLOP_PER_RAY * float(stats[0]) + FLOP_PER_WEIGHT * float(stats[3])
+    achieved = flops / fill_s / 1e12
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "fill_traffic.json")
+    if os.path.exists(tr_path):
+        with open(tr_path) as f:
+            tr = json.load(f)
+        # scale the captured per-ray traffic to this launch
+        traffic = tr.get("bytes_per_evaluated_ray", 0.0) * float(stats[0])
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded random lenses and trajectories)", "config": config,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "lcirs_new/get_lc_irs/copy_lc per curve (reference C ABI)"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                     "frac": achieved / peak_tf, "traffic": traffic,
+                     "kernel": "fill_kernel (+ overflow retries)",
+                     "flop_per_ray": FLOP_PER_RAY, "flop_per_accepted_ray": FLOP_PER_WEIGHT,
+                     "peak_source": "2 x 128 FP32 lanes x %d SMs x sm_max_mhz %.0f (MEASURED_PEAKS)"
+                                    % (sms, sm_max),
+                     "fill_ms_per_step": fill_ms / args.steps},
+        "rays": {"accepted_per_step": int(stats[3]), "evaluated_per_step": int(stats[0]),
+                 "fp64_per_step": int(stats[1]), "tiles_per_step": int(stats[2]),
+                 "accepted_per_s": float(stats[3]) * world / (ms_step / 1e3),
+                 "status_or": int(np.bitwise_or.reduce(st))},
+        "clocks": clocks,
+        "gpu_launches": 6 * args.steps,
+    }
+    if pool is not None and rank == 0:
+        pts_s, pts_s1, rays_s, desc, busy = cpu_baseline(pool, ncpu, lenses, trajs, n,
+                                                         args.cpu_sample)
+        line["cpu_baseline"] = {"value": pts_s, "unit": UNIT, "cores": ncpu, "kind": "port",
+                                "sample": desc, "value_1core": pts_s1, "rays_per_s": rays_s}
+        pool.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

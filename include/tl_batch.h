@@ -59,8 +59,11 @@ long tlb_run_host(tl_batch* b, int ntraj, const double* traj4, const int32_t* le
 int tlb_stats(tl_batch* b, uint64_t* out4);
 
 /* Ray-map precision (0 FP64 everywhere, 1 FP32 + FP64 guard band) and fill
- * launch shape (ctas <= 0 and cap_log2 <= 0 keep the current values). */
-int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads);
+ * launch shape: CTAs, log2 of the first block table's capacity in 32x8
+ * tiles, threads per CTA, rows per frontier block (8, 16 or 32).  Values
+ * <= 0 keep the current setting. */
+int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads,
+                  int block_h);
 
 /* Point-source magnifications (reference get_lc sampling t = i/(n-1)) of the
  * current trajectories, n points each, written to amp (host). */

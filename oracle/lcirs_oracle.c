@@ -188,6 +188,7 @@ struct orc_lcirs {
   int fragile;     /* set when an image decision sat near the filter radius */
   double fragile_band; /* residual below which a filter/lens-equation
                           disagreement marks the point fragile */
+  double kappa_max;    /* images with a larger sum m_i/|z - z_i|^2 are fragile */
   /* amoeba (amoeba.h) */
   orc_row *rows;
   long rows_cap, rows_used;
@@ -434,6 +435,15 @@ static int filter_images(orc_lcirs *o, const cx *roots, cx zeta, cx *imgs) {
     double r = img_residual(o, roots[k], zeta);
     if (r > 1.0e-7 && r < 1.0e-5) o->fragile = 1;
     if (r < o->fragile_band && accepted != true_image(o, roots[k], zeta)) o->fragile = 1;
+    /* an image next to a lens: the residual amplifies the root's rounding
+     * error by kappa = sum m_i/|z - z_i|^2, so implementations whose
+     * polynomial coefficients round differently accept or reject it */
+    if (r < 1.0e-2 && (accepted || true_image(o, roots[k], zeta))) {
+      cx z = roots[k];
+      double kap = o->m1 / cnorm(csub(z, o->z1)) + o->m2 / cnorm(csub(z, o->z2)) +
+                   o->m3 / cnorm(csub(z, o->z3));
+      if (kap > o->kappa_max) o->fragile = 1;
+    }
   }
   return n;
 }
@@ -791,6 +801,7 @@ orc_lcirs *orc_new(double a, double b, double th, double m2, double m3,
   o->z3 = mk(b * cos(th), b * sin(th));
   o->is_binary_img = (a == 0.0 || b == 0.0 || m3 == 0.0);
   o->fragile_band = 1.0e-4;
+  o->kappa_max = 300.0;
   o->rho = rho;
   o->rho2 = rho * rho;
   o->lc_length = lc_length;

@@ -34,7 +34,8 @@ def _bind(L):
     L.tlb_run_host.restype = ctypes.c_long
     L.tlb_stats.argtypes = [vp, ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
     L.tlb_stats.restype = ctypes.c_int
-    L.tlb_configure.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.tlb_configure.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int]
     L.tlb_configure.restype = ctypes.c_int
     L.tlb_point_lc.argtypes = [vp, f64]
     L.tlb_point_lc.restype = ctypes.c_long
@@ -61,8 +62,8 @@ class Batch:
         except Exception:
             pass
 
-    def configure(self, precision=-1, fill_ctas=0, table_log2=0, threads=0):
-        return self.L.tlb_configure(self.obj, precision, fill_ctas, table_log2, threads)
+    def configure(self, precision=-1, fill_ctas=0, table_log2=0, threads=0, block_h=0):
+        return self.L.tlb_configure(self.obj, precision, fill_ctas, table_log2, threads, block_h)
 
     def set_lenses(self, lenses):
         lenses = np.ascontiguousarray(lenses, np.float64)

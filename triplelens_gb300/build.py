@@ -76,7 +76,7 @@ def build(verbose=False):
         ins = [objs[s] for s in srcs]
         if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(o) for o in ins):
             continue
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", out] + ins
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", out] + ins + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed for %s:\n%s" % (lib, r.stderr))

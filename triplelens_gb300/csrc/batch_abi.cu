@@ -203,12 +203,13 @@ int tlb_stats(tl_batch* b, uint64_t* out4) {
   return 0;
 }
 
-int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads) {
+int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads,
+                  int block_h) {
   if (!b) return -1;
   if (precision >= 0) b->precision = precision;
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
-  E.set_fill_config(fill_ctas, table_log2, threads);
+  E.set_fill_config(fill_ctas, table_log2, threads, block_h);
   return 0;
 }
 

@@ -119,23 +119,46 @@ struct FillScratch {
   unsigned* next_point;    // work counter (1 word)
   int ctas;
   int cap_log2;
+  int block_h;             // rows per block (8, 16 or 32)
+  int rec_words;           // 32-bit words per block record
   // optional export of the filled masks: records of kDumpWords words
   // (point, tx, ty, F[8]); nullptr disables it
   uint32_t* dump;
   unsigned* dump_count;
   unsigned dump_cap;
+  // optional profiling counters (8 x u64): tiles, cycles in tiles, idle
+  // polls, cycles in work loops, super-tiles, cycles building super-tiles,
+  // cycles evaluating rays, cycles pushing
+  unsigned long long* prof;
+  // optional heartbeat in host-mapped memory: one 64-bit word per warp,
+  // (phase << 56) | (point << 24) | step (debugging of slow points)
+  unsigned long long* heartbeat;
 };
 constexpr int kDumpWords = 11;
 constexpr int kSuperLog2 = 12;   // super-tile table capacity per CTA (entries)
 
-size_t fill_scratch_bytes(int ctas, int cap_log2);
-void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, cudaStream_t st);
+int block_rec_words(int bh);
+size_t fill_scratch_bytes(int ctas, int cap_log2, int bh);
+void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, int bh,
+                       cudaStream_t st);
 
 enum FillMode : int { kFillFp64 = 0, kFillSplit = 1 };
 
+// d_list/d_count (optional): process only the listed points
 void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                  const int32_t* d_seeds, PointOut* d_out, const FillScratch& s, int mode,
-                 int threads, cudaStream_t st);
+                 int threads, cudaStream_t st, const int32_t* d_list = nullptr,
+                 const unsigned* d_count = nullptr);
+
+void launch_collect_overflow(PointOut* d_out, int npoints, int32_t* d_list, unsigned* d_count,
+                             cudaStream_t st);
+
+// block-table sizes tried in turn for points whose table overflows:
+// (CTAs, log2 of the table's capacity in 32x8 tiles); CTAs <= 0 means two
+// per SM.  A table of 2^k tiles holds 2^k / (BH/8) blocks.
+constexpr int kFillLevels = 3;
+constexpr int kFillLevelCtas[kFillLevels] = {0, 64, 16};
+constexpr int kFillLevelLog2[kFillLevels] = {17, 20, 22};
 
 int fill_default_ctas();
 

@@ -1,6 +1,11 @@
 // engine_host.cu - process-wide GPU resources of the engine (see engine_host.h).
 #include <cuda_runtime.h>
 
+#include <unistd.h>
+
+#include <atomic>
+#include <thread>
+
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -45,6 +50,13 @@ Engine::Engine() {
     sync_steps = atoi(c) >= 2;
   }
   if (const char* c = getenv("TL_FILL_CTAS")) want_ctas_ = atoi(c);
+  // TL_FILL_LEVELS=1 disables the overflow retries (and their tables)
+  if (const char* c = getenv("TL_FILL_LEVELS")) levels_ = atoi(c);
+  if (const char* c = getenv("TL_FILL_PROFILE")) profiling = atoi(c) != 0;
+  if (const char* c = getenv("TL_BLOCK_H")) {
+    const int b = atoi(c);
+    if (b == 8 || b == 16 || b == 32) block_h_ = b;
+  }
 }
 
 void Engine::trace(const char* what) {
@@ -64,26 +76,42 @@ bool Engine::check(cudaError_t e) {
   return true;
 }
 
-void Engine::set_fill_config(int ctas, int cap_log2, int threads) {
+void Engine::set_fill_config(int ctas, int cap_log2, int threads, int block_h) {
   if (ctas > 0) want_ctas_ = ctas;
   if (cap_log2 > 0) want_cap_log2_ = cap_log2;
   if (threads > 0) threads_ = threads;
-  if (fs_.keys && (fs_.ctas != want_ctas_ || fs_.cap_log2 != want_cap_log2_)) {
-    cudaStreamSynchronize(stream);
-    cudaFree(fill_base_);
-    fill_base_ = nullptr;
-    fs_ = FillScratch{};
+  const bool bh_changed = (block_h == 8 || block_h == 16 || block_h == 32) && block_h != block_h_;
+  if (bh_changed) block_h_ = block_h;
+  for (int level = 0; level < kFillLevels; level++) {
+    if (!fs_[level].keys) continue;
+    if (bh_changed || (level == 0 && (fs_[0].ctas != want_ctas_ ||
+                                      fs_[0].cap_log2 + (block_h_ == 32 ? 2 : (block_h_ == 16 ? 1 : 0)) !=
+                                          want_cap_log2_))) {
+      cudaStreamSynchronize(stream);
+      cudaFree(fill_base_[level]);
+      fill_base_[level] = nullptr;
+      fs_[level] = FillScratch{};
+    }
   }
 }
 
-void Engine::ensure_fill_scratch() {
-  if (fs_.keys) return;
-  const int ctas = want_ctas_ > 0 ? want_ctas_ : fill_default_ctas();
-  const int cap = want_cap_log2_;
-  fill_bytes_ = fill_scratch_bytes(ctas, cap);
-  if (!check(cudaMalloc(&fill_base_, fill_bytes_))) return;
-  fill_scratch_init(&fs_, fill_base_, ctas, cap, stream);
+bool Engine::ensure_fill_scratch(int level) {
+  if (fs_[level].keys) return true;
+  int ctas, cap;
+  if (level == 0) {
+    ctas = want_ctas_ > 0 ? want_ctas_ : fill_default_ctas();
+    cap = want_cap_log2_;
+  } else {
+    ctas = kFillLevelCtas[level];
+    cap = kFillLevelLog2[level];
+  }
+  // capacities are counted in 32x8 tiles; a block holds block_h/8 of them
+  for (int b = block_h_; b > 8; b >>= 1) cap--;
+  const size_t bytes = fill_scratch_bytes(ctas, cap, block_h_);
+  if (!check(cudaMalloc(&fill_base_[level], bytes))) return false;
+  fill_scratch_init(&fs_[level], fill_base_[level], ctas, cap, block_h_, stream);
   check(cudaStreamSynchronize(stream));
+  return true;
 }
 
 Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump) {
@@ -113,12 +141,81 @@ void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
 }
 
 void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
-  ensure_fill_scratch();
-  FillScratch s = fs_;
+  if (!ensure_fill_scratch(0)) return;
+  FillScratch s = fs_[0];
   s.dump = R.dump;
   s.dump_count = R.dump_count;
   s.dump_cap = R.dump_cap;
+  unsigned long long* prof = nullptr;
+  if (profiling) {
+    prof = (unsigned long long*)prof_.need(8 * sizeof(unsigned long long));
+    cudaMemsetAsync(prof, 0, 8 * sizeof(unsigned long long), st);
+    s.prof = prof;
+  }
+  if (heartbeat_words_ == 0 && getenv("TL_HEARTBEAT")) {
+    heartbeat_words_ = 1 << 16;
+    cudaHostAlloc((void**)&heartbeat_host_, heartbeat_words_ * 8, cudaHostAllocMapped);
+    cudaHostGetDevicePointer((void**)&heartbeat_dev_, heartbeat_host_, 0);
+  }
+  s.heartbeat = heartbeat_dev_;
   launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st);
+  if (heartbeat_host_) {
+    // a side thread reports the warps' phases while the stream is busy; the
+    // caller keeps blocking as usual
+    const int nw = s.ctas * (threads_ / 32);
+    unsigned long long* hb = heartbeat_host_;
+    std::atomic<bool> done(false);
+    std::thread watch([hb, nw, &done]() {
+      for (int it = 1; !done.load() && it < 600; it++) {
+        for (int k = 0; k < 20 && !done.load(); k++) usleep(100000);
+        if (done.load()) break;
+        int hist[16] = {0};
+        for (int w = 0; w < nw; w++) hist[(hb[w] >> 56) & 15]++;
+        fprintf(stderr, "[tl hb] %ds phases:", 2 * it);
+        for (int k = 0; k < 9; k++) fprintf(stderr, " %d:%d", k, hist[k]);
+        fprintf(stderr, "\n");
+        int shown = 0;
+        for (int w = 0; w < nw && shown < 16; w++) {
+          const unsigned long long v = hb[w];
+          const int ph = (int)((v >> 56) & 15);
+          if (ph != 0 && ph != 8) {
+            fprintf(stderr, "   warp %d cta %d phase %d point %llu step %llu\n", w, w / 8, ph,
+                    (v >> 24) & 0xffffffffull, v & 0xffffffull);
+            shown++;
+          }
+        }
+      }
+    });
+    cudaStreamSynchronize(st);
+    done.store(true);
+    watch.join();
+  }
+  if (profiling) {
+    unsigned long long h[8];
+    cudaMemcpyAsync(h, prof, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    fprintf(stderr,
+            "[tl prof] tiles %llu  cyc/tile %.0f  idle polls %llu  work-loop cyc %llu  "
+            "supertiles %llu  cyc/supertile %.0f  eval cyc/tile %.0f  push cyc/tile %.0f\n",
+            h[0], h[0] ? (double)h[1] / h[0] : 0.0, h[2], h[3], h[4],
+            h[4] ? (double)h[5] / h[4] : 0.0, h[0] ? (double)h[6] / h[0] : 0.0,
+            h[0] ? (double)h[7] / h[0] : 0.0);
+  }
+  // points whose tile table overflowed run again with larger tables; the
+  // retry launches read their point count on the device, so no host round
+  // trip is needed (a retry with an empty list exits at once)
+  char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
+  int32_t* list = (int32_t*)(rb + 64);
+  unsigned* count = (unsigned*)rb;
+  for (int level = 1; level < kFillLevels && level < levels_; level++) {
+    if (!ensure_fill_scratch(level)) break;
+    FillScratch sl = fs_[level];
+    sl.dump = R.dump;
+    sl.dump_count = R.dump_count;
+    sl.dump_cap = R.dump_cap;
+    launch_collect_overflow(R.out, (int)np, list, count, st);
+    launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, sl, mode, threads_, st, list, count);
+  }
   check(cudaGetLastError());
 }
 

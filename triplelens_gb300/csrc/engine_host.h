@@ -48,18 +48,26 @@ class Engine {
   void trace(const char* what);
   bool tracing = false;
   bool sync_steps = false;  // TL_TRACE=2: also synchronise after every launch
-  int fill_ctas() const { return fs_.ctas; }
-  int fill_cap_log2() const { return fs_.cap_log2; }
-  void set_fill_config(int ctas, int cap_log2, int threads);
+  bool profiling = false;   // TL_FILL_PROFILE=1: fill-kernel cycle counters
+  int fill_ctas() const { return fs_[0].ctas; }
+  int fill_cap_log2() const { return fs_[0].cap_log2; }
+  // fill launch shape; values <= 0 keep the current setting; block_h is the
+  // rows per block (8, 16 or 32)
+  void set_fill_config(int ctas, int cap_log2, int threads, int block_h = 0);
+  int block_h() const { return block_h_; }
 
  private:
   Engine();
-  void ensure_fill_scratch();
-  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_;
-  void* fill_base_ = nullptr;
-  size_t fill_bytes_ = 0;
-  FillScratch fs_{};
+  bool ensure_fill_scratch(int level);
+  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_;
+  void* fill_base_[kFillLevels] = {nullptr, nullptr, nullptr};
+  FillScratch fs_[kFillLevels]{};
   int want_ctas_ = 0, want_cap_log2_ = 17, threads_ = 256;
+  int levels_ = kFillLevels;
+  size_t heartbeat_words_ = 0;
+  unsigned long long* heartbeat_host_ = nullptr;
+  unsigned long long* heartbeat_dev_ = nullptr;
+  int block_h_ = 32;
 };
 
 }  // namespace tl

@@ -1,5 +1,6 @@
 // fill.cu - persistent amoeba kernel: the filled set of every source
-// position, grown as a frontier of 32x8 ray tiles.
+// position, grown as a frontier of ray blocks (32 columns x BH rows, made of
+// BH/8 tiles of 32x8 rays; BH in {8, 16, 32} is chosen by the autotuner).
 //
 // What it computes (lcirs.cc:171-174 + lineFloodFill lcirs.cc:381-466 +
 // Amoeba amoeba.cc:15-82): the union of the 4-connected components (same row
@@ -10,22 +11,24 @@
 //
 // Layout:
 //   * one CTA works on one source position at a time, taking positions from
-//     a global counter (persistent grid, a few CTAs per SM);
-//   * per CTA a tile table in HBM: 64-bit tile keys (open addressing,
-//     linear probing) and 128-byte tile records holding the pending entry
-//     bits (seeds, bottom row, top row, left/right columns), the tile state
-//     (QUEUED/BUSY), the accepted mask H (8 rows x 32 bits) and the filled
-//     mask F;
-//   * per CTA a work ring of tile slots; counters live in shared memory.
-// A warp processes one tile: lane = column, 8 rows per lane; __ballot_sync
-// builds the 8 row masks; the closure of the entry bits inside the tile is a
-// bit-parallel run fill (carry propagation) plus shuffles between rows;
-// newly filled border bits are pushed to the four neighbour tiles.  Closure
-// distributes over union, so the order in which tiles and entries are
-// processed does not change the result.
+//     a global counter (persistent grid, two CTAs per SM);
+//   * per CTA a block table in HBM: 64-bit block keys (open addressing,
+//     linear probing, one CAS per probe) and block records holding the
+//     pending entry bits (seed rows, bottom row, top row, left and right
+//     columns), a state word (queued | busy | accepted-mask-done), the
+//     accepted mask H (BH rows x 32 bits), the filled mask F and the F
+//     column summaries used to filter pushes;
+//   * per CTA a work ring of block slots; counters in shared memory.
+// A warp processes one block: lane = column, BH rays per lane; a ballot per
+// row builds the accepted masks; lane r < BH then holds row r, and the
+// closure of the entry bits is a bit-parallel run fill (carry propagation)
+// with shuffles between neighbouring rows; newly filled border bits are
+// pushed to the four neighbour blocks.  Closure distributes over union, so
+// the processing order of blocks and entries does not change the result.
 //
 // Every wait is bounded: an expired wait sets kStTimeout on the point and the
-// CTA abandons that point.  A full table sets kStTableFull.
+// CTA abandons that point.  A full table sets kStTableFull (the host retries
+// those points with larger tables).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -36,27 +39,34 @@ namespace tl {
 namespace {
 
 constexpr uint64_t kEmptyKey = ~0ull;
-constexpr int kRecWords = 32;
-// record layout (32-bit words)
-constexpr int kRSeed = 0;    // [0..7]  seed entry bits per row
-constexpr int kRBot = 8;     // entries into row 0 from the tile below
-constexpr int kRTop = 9;     // entries into row 7 from the tile above
-constexpr int kRLR = 10;     // bits 0-7: column 0 per row; bits 8-15: column 31
-constexpr int kRState = 11;  // kQueued | kBusy
-constexpr int kRHDone = 12;  // H computed
-constexpr int kRH = 16;      // [16..23] accepted mask
-constexpr int kRF = 24;      // [24..31] filled mask
-constexpr uint32_t kQueued = 1u, kBusy = 2u;
+constexpr uint32_t kQ = 1u, kB = 2u, kD = 4u;   // queued, busy, H done
+
+template <int BH>
+struct Lo {
+  static constexpr int kBot = BH, kTop = BH + 1, kLeft = BH + 2, kRight = BH + 3;
+  static constexpr int kState = BH + 4, kFl = BH + 5, kFr = BH + 6;
+  static constexpr int kH = BH + 8, kF = 2 * BH + 8;
+  static constexpr int kWords = (3 * BH + 8) <= 32 ? 32 : ((3 * BH + 8) <= 64 ? 64 : 128);
+};
 
 constexpr unsigned kIdleSpinLimit = 1u << 21;   // x ~100 ns sleeps
-constexpr unsigned long long kPointDeadlineNs = 20ull * 1000000000ull;  // per point
+constexpr unsigned kEntrySpinLimit = 1u << 20;
+constexpr unsigned long long kPointDeadlineNs = 5ull * 1000000000ull;  // per point
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-constexpr unsigned kEntrySpinLimit = 1u << 20;
+
+__device__ __forceinline__ void beat(unsigned long long* hb, int phase, int point, unsigned step) {
+  if (hb) {
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    *(volatile unsigned long long*)&hb[w] =
+        ((unsigned long long)phase << 56) | ((unsigned long long)(point & 0xffffffff) << 24) |
+        (step & 0xffffff);
+  }
+}
 
 struct Ctx {
   double sx, sy;
@@ -78,9 +88,21 @@ struct Shared {
   unsigned abort_, status;
   unsigned long long count, wsum, rays_eval, rays_fp64;
   unsigned long long t0;
-  unsigned dbg_again, dbg_state, dbg_slot, dbg_deq, max_pass;
+  unsigned dbg_again, dbg_deq, max_pass, profiling, dbg_where;
+  unsigned long long prof[8];  // profiling counters (sc.prof != nullptr)
+  unsigned long long* hb;
   int point;
 };
+
+// true (and the point aborted, with `where` recorded) once the point has run
+// past its deadline
+__device__ __forceinline__ bool overdue(Shared& S, unsigned where) {
+  if (globaltimer() - S.t0 <= kPointDeadlineNs) return false;
+  atomicCAS(&S.dbg_where, 0u, where);
+  atomicOr(&S.status, kStTimeout);
+  atomicExch(&S.abort_, 1u);
+  return true;
+}
 
 __device__ __forceinline__ uint32_t ldcg32(const uint32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ uint64_t ldcg64(const uint64_t* p) {
@@ -102,7 +124,7 @@ __device__ __forceinline__ uint32_t hash_key(uint64_t k) {
 
 // FP64 ray map in the reference's irsSIMD lane order (lcirs.cc:290-341):
 // lanes (z3, z2, z1, zeta_s); every operation separately rounded.
-__device__ __forceinline__ double irs_exact(const Ctx& c, double x, double y) {
+__device__ __noinline__ double irs_exact(const Ctx& c, double x, double y) {
   if (c.binary) {
     // irsBinary (lcirs.cc:345-353) with the naive complex division
     cx img = mk(x, y);
@@ -169,6 +191,7 @@ struct Table {
   uint32_t* ring;
   uint32_t* used;
   uint32_t mask;
+  int rec_words;
   uint64_t* skeys;
   uint32_t* sents;
   uint32_t* sused;
@@ -180,25 +203,22 @@ __device__ __forceinline__ void set_abort(Shared& S, uint32_t st) {
   atomicExch(&S.abort_, 1u);
 }
 
-// find or insert tile (tx, ty); returns the slot or -1 (table full / abort)
-__device__ int find_or_insert(Shared& S, const Table& T, int tx, int ty) {
-  const uint64_t key = tile_key(tx, ty);
+// find or insert block (bx, by): one CAS per probe; -1 if the table is full
+__device__ __noinline__ int find_or_insert(Shared& S, const Table& T, int bx, int by) {
+  const uint64_t key = tile_key(bx, by);
   uint32_t i = hash_key(key) & T.mask;
   for (uint32_t probe = 0; probe <= T.mask; probe++, i = (i + 1) & T.mask) {
-    uint64_t k = ldcg64(&T.keys[i]);
-    if (k == key) return (int)i;
-    if (k == kEmptyKey) {
-      unsigned long long old =
-          atomicCAS((unsigned long long*)&T.keys[i], (unsigned long long)kEmptyKey,
-                    (unsigned long long)key);
-      if (old == kEmptyKey) {
-        const unsigned u = atomicAdd(&S.used, 1u);
-        __stcg(&T.used[u], i);  // u < capacity: at most mask+1 slots exist
-        if (u >= (T.mask + 1) / 4 * 3) set_abort(S, kStTableFull);
-        return (int)i;
-      }
-      if (old == key) return (int)i;
+    if ((probe & 255) == 255 && overdue(S, 1)) return -1;
+    const unsigned long long old = atomicCAS((unsigned long long*)&T.keys[i],
+                                             (unsigned long long)kEmptyKey,
+                                             (unsigned long long)key);
+    if (old == kEmptyKey) {
+      const unsigned u = atomicAdd(&S.used, 1u);
+      __stcg(&T.used[u], i);  // u < capacity: at most mask+1 slots exist
+      if (u >= (T.mask + 1) / 4 * 3) set_abort(S, kStTableFull);
+      return (int)i;
     }
+    if (old == key) return (int)i;
   }
   set_abort(S, kStTableFull);
   return -1;
@@ -210,45 +230,47 @@ __device__ __forceinline__ void enqueue(Shared& S, const Table& T, int slot) {
   atomicExch(&T.ring[t & T.mask], (uint32_t)slot + 1u);
 }
 
-// one lane: OR entry bits into word `w` of tile (tx, ty) and queue it
-__device__ void push(Shared& S, const Table& T, int tx, int ty, int w, uint32_t bits) {
+enum PushKind { kPushSeed = 0, kPushBot, kPushTop, kPushLeft, kPushRight };
+
+// one lane: post entry bits into block (bx, by) and queue it.  `row` is the
+// row of a seed entry.  Bits that the target has already filled are dropped
+// (the F rows and the F column summaries are read for that).
+template <int BH>
+__device__ __noinline__ void push(Shared& S, const Table& T, int bx, int by, int kind, int row,
+                                  uint32_t bits) {
+  using L = Lo<BH>;
   if (!bits) return;
-  if (tx < 0 || ty < 0 || tx > S.c.txmax || ty > S.c.tymax) return;
+  if (bx < 0 || by < 0 || bx > S.c.txmax || by > S.c.tymax) return;
   if (S.abort_) return;
-  const int slot = find_or_insert(S, T, tx, ty);
+  const int slot = find_or_insert(S, T, bx, by);
   if (slot < 0) return;
-  uint32_t* rec = T.recs + (size_t)slot * kRecWords;
-  // entries that are already filled add nothing
-  if (w == kRBot) {
-    bits &= ~ldcg32(&rec[kRF + 0]);
-  } else if (w == kRTop) {
-    bits &= ~ldcg32(&rec[kRF + 7]);
-  } else if (w == kRLR) {
-    uint32_t keep = 0;
-    for (int r = 0; r < 8; r++) {
-      const uint32_t f = ldcg32(&rec[kRF + r]);
-      if (((bits >> r) & 1u) && !(f & 1u)) keep |= 1u << r;
-      if (((bits >> (8 + r)) & 1u) && !(f & 0x80000000u)) keep |= 1u << (8 + r);
-    }
-    bits = keep;
-  } else {
-    bits &= ~ldcg32(&rec[kRF + (w - kRSeed)]);
+  uint32_t* rec = T.recs + (size_t)slot * T.rec_words;
+  int w;
+  uint32_t filled;
+  switch (kind) {
+    case kPushBot: w = L::kBot; filled = ldcg32(&rec[L::kF + 0]); break;
+    case kPushTop: w = L::kTop; filled = ldcg32(&rec[L::kF + BH - 1]); break;
+    case kPushLeft: w = L::kLeft; filled = ldcg32(&rec[L::kFl]); break;
+    case kPushRight: w = L::kRight; filled = ldcg32(&rec[L::kFr]); break;
+    default: w = row; filled = ldcg32(&rec[L::kF + row]); break;
   }
+  bits &= ~filled;
   if (!bits) return;
   atomicOr(&rec[w], bits);
   __threadfence_block();
-  const uint32_t old = atomicOr(&rec[kRState], kQueued);
-  if (old == 0u) enqueue(S, T, slot);
+  const uint32_t old = atomicOr(&rec[L::kState], kQ);
+  if ((old & (kQ | kB)) == 0u) enqueue(S, T, slot);
 }
 
 // lane 0: take one slot from the ring; -1 if the ring is empty
-__device__ int try_dequeue(Shared& S, const Table& T) {
+__device__ __noinline__ int try_dequeue(Shared& S, const Table& T) {
   for (unsigned spin = 0;; spin++) {
     if (spin > (1u << 22)) {
       atomicAdd(&S.dbg_deq, 1u);
       set_abort(S, kStTimeout);
       return -1;
     }
+    if ((spin & 1023) == 1023 && overdue(S, 2)) return -1;
     const unsigned h = *(volatile unsigned*)&S.head;
     const unsigned t = *(volatile unsigned*)&S.tail;
     if (h == t) return -1;
@@ -256,6 +278,7 @@ __device__ int try_dequeue(Shared& S, const Table& T) {
       unsigned v;
       unsigned it = 0;
       while ((v = atomicExch(&T.ring[h & T.mask], 0u)) == 0u) {
+        if ((it & 255) == 255 && overdue(S, 3)) return -1;
         if (++it > kEntrySpinLimit) {
           set_abort(S, kStTimeout);
           return -1;
@@ -267,28 +290,16 @@ __device__ int try_dequeue(Shared& S, const Table& T) {
   }
 }
 
-// Evaluates the 8 rays of this lane's column in tile (tx, ty) in FP64.
-// Returns the 8 row masks (uniform) and keeps each ray's weight in w[].
-__device__ __forceinline__ void eval_tile_fp64(const Ctx& c, int tx, int ty, int lane,
-                                               uint32_t* H, double* w, unsigned* nrays) {
-  const int64_t nx = (int64_t)tx * 32 + lane;
-  const bool col_ok = nx >= 1 && nx <= c.n - 1;
-  const double x = grid_x(c, nx);
-  unsigned evaluated = 0;
+__device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
-    const int64_t ny = (int64_t)ty * 8 + r;
-    bool hit = false;
-    w[r] = 0.0;
-    if (col_ok && ny <= c.n - 1) {
-      const double rsq = irs_exact(c, x, grid_y(c, ny));
-      evaluated++;
-      hit = rsq < c.rho2;
-      if (hit) w[r] = ray_weight(c, rsq);
-    }
-    H[r] = __ballot_sync(0xffffffffu, hit);
-  }
-  *nrays = evaluated;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -308,6 +319,7 @@ __device__ __forceinline__ void eval_tile_fp64(const Ctx& c, int tx, int ty, int
 // is below u*rho/2; where no K qualifies, the exact difference form
 //   s = D0 + delta + sum_i m_i conj(delta / ((W_i + delta) W_i))
 // is used in FP32, and where a lens lies inside the super-tile, FP64.
+// K is rounded up to 2, 4 or 8 (three compiled variants).
 // From the magnitudes of the terms the super-tile also gets an error bound E
 // on s and a band B = 4 rho E + 4 E^2 + 4 u rho^2 on r^2: a ray with
 // |r^2 - rho^2| <= B is classified by the exact FP64 map (irs_exact), so the
@@ -331,7 +343,7 @@ __device__ __forceinline__ double shfl_d(double v, int src) {
 }
 
 // whole warp: computes the entry of super-tile (sx, sy) into `ent`
-__device__ void compute_supertile(const Ctx& c, int sxi, int syi, int lane, uint32_t* ent) {
+__device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, int lane, uint32_t* ent) {
   const int half = 1 << (c.slog2 - 1);
   const int64_t nxc = ((int64_t)sxi << c.slog2) + half;
   const int64_t nyc = ((int64_t)syi << c.slog2) + half;
@@ -399,6 +411,9 @@ __device__ void compute_supertile(const Ctx& c, int sxi, int syi, int lane, uint
     for (int k = 1; k <= 8; k++)
       if (tk[k] <= 0.5 * u * c.rho) { K = k; break; }
   }
+  // three compiled orders keep the kernel's code small: round K up to 2, 4
+  // or 8 (more terms only shrink the tail)
+  if (K > 0) K = K <= 2 ? 2 : (K <= 4 ? 4 : 8);
   if (K > 0) {
     double sc = 0.0, dp = dmax;
     for (int n = 0; n < K; n++) {
@@ -434,12 +449,12 @@ __device__ void compute_supertile(const Ctx& c, int sxi, int syi, int lane, uint
 }
 
 // find-or-compute the super-tile holding tile (tx, ty); whole warp
-__device__ bool get_supertile(Shared& S, const Table& T, int tx, int ty, int lane,
-                              SuperTile* st) {
+__device__ __noinline__ bool get_supertile(Shared& S, const Table& T, int64_t nx0, int64_t ny0,
+                                           int lane, SuperTile* st) {
   const Ctx& c = S.c;
   const int sh = c.slog2;
-  const int sxi = (int)(((int64_t)tx * 32) >> sh);
-  const int syi = (int)(((int64_t)ty * 8) >> sh);
+  const int sxi = (int)(nx0 >> sh);
+  const int syi = (int)(ny0 >> sh);
   const uint64_t key = tile_key(sxi, syi);
   int slot = -1, mine = 0;
   if (lane == 0) {
@@ -468,13 +483,16 @@ __device__ bool get_supertile(Shared& S, const Table& T, int tx, int ty, int lan
   if (slot < 0) return false;
   uint32_t* ent = T.sents + (size_t)slot * kSEntryWords;
   if (mine) {
+    const long long c0 = clock64();
     compute_supertile(c, sxi, syi, lane, ent);
     if (lane == 0) atomicExch(&ent[kSState], 2u);
+    if (lane == 0 && S.profiling) atomicAdd(&S.prof[5], (unsigned long long)(clock64() - c0));
   } else {
     uint32_t ready = 0;
     if (lane == 0) {
       for (unsigned it = 0; it < (1u << 18); it++) {
         if (atomicAdd(&ent[kSState], 0u) == 2u) { ready = 1; break; }
+        if ((it & 255) == 255 && overdue(S, 4)) break;
         __nanosleep(64);
       }
     }
@@ -502,285 +520,335 @@ __device__ bool get_supertile(Shared& S, const Table& T, int tx, int ty, int lan
 }
 
 template <int K>
-__device__ __forceinline__ void taylor_rows(const SuperTile& st, float ex, float bx,
-                                            const float* dyr, float* r2) {
+__device__ __forceinline__ float taylor_r2(const SuperTile& st, float ex, float bx, float dy) {
+  const float ey = -dy;
+  float pr = st.cr[K - 1], pi = st.ci[K - 1];
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
-    const float ey = -dyr[r];
-    float pr = st.cr[K - 1], pi = st.ci[K - 1];
-#pragma unroll
-    for (int n = K - 2; n >= 0; n--) {
-      const float tr = fmaf(pr, ex, fmaf(-pi, ey, st.cr[n]));
-      const float ti = fmaf(pr, ey, fmaf(pi, ex, st.ci[n]));
-      pr = tr;
-      pi = ti;
-    }
-    const float qr = fmaf(pr, ex, -pi * ey);
-    const float qi = fmaf(pr, ey, pi * ex);
-    const float sx = bx - qr;
-    const float sy = (st.d0y + dyr[r]) - qi;
-    r2[r] = fmaf(sx, sx, sy * sy);
+  for (int n = K - 2; n >= 0; n--) {
+    const float tr = fmaf(pr, ex, fmaf(-pi, ey, st.cr[n]));
+    const float ti = fmaf(pr, ey, fmaf(pi, ex, st.ci[n]));
+    pr = tr;
+    pi = ti;
   }
+  const float qr = fmaf(pr, ex, -pi * ey);
+  const float qi = fmaf(pr, ey, pi * ex);
+  const float sx = bx - qr;
+  const float sy = (st.d0y + dy) - qi;
+  return fmaf(sx, sx, sy * sy);
 }
 
-__device__ __forceinline__ void exact32_rows(const Ctx& c, const SuperTile& st, float dx,
-                                             float bx, const float* dyr, float* r2) {
-  const float ms[3] = {(float)c.m1, (float)c.m2, (float)c.m3};
+__device__ __forceinline__ float exact32_r2(const Ctx& c, const SuperTile& st, float dx, float bx,
+                                            float dy) {
+  float sx = bx, sy = st.d0y + dy;
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
-    const float dy = dyr[r];
-    float sx = bx, sy = st.d0y + dy;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const float wx = st.cr[i], wy = st.ci[i];
-      const float vx = wx + dx, vy = wy + dy;
-      const float px = vx * wx - vy * wy, py = vx * wy + vy * wx;   // P = V W
-      const float inv = __frcp_rn(fmaf(px, px, py * py));
-      const float qx = (dx * px + dy * py) * inv, qy = (dy * px - dx * py) * inv;  // delta/P
-      sx = fmaf(ms[i], qx, sx);
-      sy = fmaf(-ms[i], qy, sy);   // + m conj(delta/P)
-    }
-    r2[r] = fmaf(sx, sx, sy * sy);
+  for (int i = 0; i < 3; i++) {
+    const float mi = i == 0 ? (float)c.m1 : (i == 1 ? (float)c.m2 : (float)c.m3);
+    const float wx = st.cr[i], wy = st.ci[i];
+    const float vx = wx + dx, vy = wy + dy;
+    const float px = vx * wx - vy * wy, py = vx * wy + vy * wx;   // P = V W
+    const float inv = __frcp_rn(fmaf(px, px, py * py));
+    const float qx = (dx * px + dy * py) * inv, qy = (dy * px - dx * py) * inv;  // delta/P
+    sx = fmaf(mi, qx, sx);
+    sy = fmaf(-mi, qy, sy);   // + m conj(delta/P)
   }
+  return fmaf(sx, sx, sy * sy);
 }
 
-// Evaluates the 8 rays of this lane's column in tile (tx, ty) with the
-// split-precision map; rays inside the guard band go through irs_exact.
-__device__ __forceinline__ void eval_tile_split(const Ctx& c, const SuperTile& st, int tx, int ty,
-                                                int lane, uint32_t* H, float* w, unsigned* nrays,
-                                                unsigned* nfp64) {
-  const int64_t nx = (int64_t)tx * 32 + lane;
+template <int K>
+__device__ __forceinline__ float split_r2(const Ctx& c, const SuperTile& st, float dx, float bx,
+                                          float dy) {
+  if (K == 0) return exact32_r2(c, st, dx, bx, dy);
+  return taylor_r2<(K > 0 ? K : 1)>(st, dx, bx, dy);
+}
+
+__device__ __forceinline__ float ld_weight_f(const Ctx& c, float r2) {
+  return fmaf(c.ldbf, sqrtf(fmaxf(0.f, fmaf(-r2, c.inv_rho2f, 1.f))), c.ldaf);
+}
+
+// Rays of this lane's column in block (bx, by), split-precision map with the
+// FP64 guard band.  Returns the accepted mask of row `lane` (lane < BH) and
+// adds the weights of this lane's accepted rays to *wsum.
+template <int BH, int K>
+__device__ __forceinline__ uint32_t classify_block(const Ctx& c, const SuperTile st, int bx,
+                                                   int by, int lane, float* wsum, unsigned* ev,
+                                                   unsigned* e64) {
+  const int64_t nx = (int64_t)bx * 32 + lane;
   const bool col_ok = nx >= 1 && nx <= c.n - 1;
   const float dx = c.hf * (float)(int)(nx - st.nxc);
-  const float bx = st.d0x + dx;
-  float dyr[8], r2[8];
-#pragma unroll
-  for (int r = 0; r < 8; r++) dyr[r] = c.hf * (float)(int)((int64_t)ty * 8 + r - st.nyc);
-  if (st.mode == kModeTaylor) {
-    switch (st.K) {
-      case 1: taylor_rows<1>(st, dx, bx, dyr, r2); break;
-      case 2: taylor_rows<2>(st, dx, bx, dyr, r2); break;
-      case 3: taylor_rows<3>(st, dx, bx, dyr, r2); break;
-      case 4: taylor_rows<4>(st, dx, bx, dyr, r2); break;
-      case 5: taylor_rows<5>(st, dx, bx, dyr, r2); break;
-      case 6: taylor_rows<6>(st, dx, bx, dyr, r2); break;
-      case 7: taylor_rows<7>(st, dx, bx, dyr, r2); break;
-      default: taylor_rows<8>(st, dx, bx, dyr, r2); break;
-    }
-  } else {
-    exact32_rows(c, st, dx, bx, dyr, r2);
-  }
-  unsigned ev = 0, e64 = 0;
+  const float bxo = st.d0x + dx;
   const float lo = c.rho2f - st.band, hi = c.rho2f + st.band;
-#pragma unroll
-  for (int r = 0; r < 8; r++) {
-    const int64_t ny = (int64_t)ty * 8 + r;
+  const int64_t ny0 = (int64_t)by * BH;
+  const int rows_ok = (int)min((int64_t)BH, c.n - ny0);  // rows <= N-1
+  uint32_t hl = 0;
+  float ws = 0.f;
+  unsigned nev = 0, n64 = 0;
+#pragma unroll 4
+  for (int r = 0; r < BH; r++) {
+    const float dy = c.hf * (float)(int)(ny0 + r - st.nyc);
+    const float r2 = split_r2<K>(c, st, dx, bxo, dy);
     bool hit = false;
-    w[r] = 0.f;
-    if (col_ok && ny <= c.n - 1) {
-      ev++;
-      if (r2[r] < lo) {
+    if (col_ok && r < rows_ok) {
+      nev++;
+      if (r2 < lo) {
         hit = true;
-        w[r] = fmaf(c.ldbf, sqrtf(fmaxf(0.f, fmaf(-r2[r], c.inv_rho2f, 1.f))), c.ldaf);
-      } else if (r2[r] <= hi) {
-        const double rsq = irs_exact(c, grid_x(c, nx), grid_y(c, ny));
-        e64++;
+        ws += ld_weight_f(c, r2);
+      } else if (r2 <= hi) {
+        const double rsq = irs_exact(c, grid_x(c, nx), grid_y(c, ny0 + r));
+        n64++;
         hit = rsq < c.rho2;
-        if (hit) w[r] = (float)ray_weight(c, rsq);
+        if (hit) ws += (float)ray_weight(c, rsq);
       }
     }
-    H[r] = __ballot_sync(0xffffffffu, hit);
+    const uint32_t b = __ballot_sync(0xffffffffu, hit);
+    if (lane == r) hl = b;
   }
-  *nrays = ev;
-  *nfp64 = e64;
+  *wsum += ws;
+  *ev += nev;
+  *e64 += n64;
+  return hl;
 }
 
-// FP32 weight of one accepted ray (re-visit of a tile whose rays are no
-// longer in registers)
-__device__ __forceinline__ float weight_split(const Ctx& c, const SuperTile& st, int64_t nx,
-                                              int64_t ny) {
-  const float dx = c.hf * (float)(int)(nx - st.nxc);
-  float dyr[8], r2[8];
-  for (int r = 0; r < 8; r++) dyr[r] = c.hf * (float)(int)(ny - st.nyc);
-  const float bx = st.d0x + dx;
-  if (st.mode == kModeTaylor) {
-    switch (st.K) {
-      case 1: taylor_rows<1>(st, dx, bx, dyr, r2); break;
-      case 2: taylor_rows<2>(st, dx, bx, dyr, r2); break;
-      case 3: taylor_rows<3>(st, dx, bx, dyr, r2); break;
-      case 4: taylor_rows<4>(st, dx, bx, dyr, r2); break;
-      case 5: taylor_rows<5>(st, dx, bx, dyr, r2); break;
-      case 6: taylor_rows<6>(st, dx, bx, dyr, r2); break;
-      case 7: taylor_rows<7>(st, dx, bx, dyr, r2); break;
-      default: taylor_rows<8>(st, dx, bx, dyr, r2); break;
+template <int BH>
+__device__ __forceinline__ uint32_t classify_block_fp64(const Ctx& c, int bx, int by, int lane,
+                                                        float* wsum, unsigned* ev,
+                                                        unsigned* e64) {
+  const int64_t nx = (int64_t)bx * 32 + lane;
+  const bool col_ok = nx >= 1 && nx <= c.n - 1;
+  const double x = grid_x(c, nx);
+  const int64_t ny0 = (int64_t)by * BH;
+  uint32_t hl = 0;
+  float ws = 0.f;
+  unsigned nev = 0;
+#pragma unroll 1
+  for (int r = 0; r < BH; r++) {
+    const int64_t ny = ny0 + r;
+    bool hit = false;
+    if (col_ok && ny <= c.n - 1) {
+      const double rsq = irs_exact(c, x, grid_y(c, ny));
+      nev++;
+      hit = rsq < c.rho2;
+      if (hit) ws += (float)ray_weight(c, rsq);
     }
-  } else {
-    exact32_rows(c, st, dx, bx, dyr, r2);
+    const uint32_t b = __ballot_sync(0xffffffffu, hit);
+    if (lane == r) hl = b;
   }
-  return fmaf(c.ldbf, sqrtf(fmaxf(0.f, fmaf(-r2[0], c.inv_rho2f, 1.f))), c.ldaf);
+  *wsum += ws;
+  *ev += nev;
+  *e64 += nev;
+  return hl;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// weight of one accepted ray evaluated again (blocks filled over several
+// passes: their rays are no longer in registers)
+__device__ __noinline__ float weight_again(const Ctx& c, const SuperTile& st, bool split,
+                                           int64_t nx, int64_t ny) {
+  if (!split || st.mode == kModeFp64) {
+    return (float)ray_weight(c, irs_exact(c, grid_x(c, nx), grid_y(c, ny)));
+  }
+  const float dx = c.hf * (float)(int)(nx - st.nxc);
+  const float dy = c.hf * (float)(int)(ny - st.nyc);
+  const float bx = st.d0x + dx;
+  float r2;
+  if (st.mode == kModeTaylor) {
+    r2 = st.K <= 2 ? taylor_r2<2>(st, dx, bx, dy)
+                   : (st.K <= 4 ? taylor_r2<4>(st, dx, bx, dy) : taylor_r2<8>(st, dx, bx, dy));
+  } else {
+    r2 = exact32_r2(c, st, dx, bx, dy);
+  }
+  return ld_weight_f(c, r2);
 }
 
-__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// per-warp cache of the last super-tile used
+struct WarpST {
+  uint64_t key;
+  bool valid;
+  SuperTile st;
+};
+
+template <int BH>
+__device__ __forceinline__ bool warp_supertile(Shared& S, const Table& T, int bx, int by,
+                                               int lane, WarpST& ws) {
+  const int sh = S.c.slog2;
+  const int64_t nx0 = (int64_t)bx * 32, ny0 = (int64_t)by * BH;
+  const uint64_t key = tile_key((int)(nx0 >> sh), (int)(ny0 >> sh));
+  if (ws.valid && ws.key == key) return true;
+  ws.valid = get_supertile(S, T, nx0, ny0, lane, &ws.st);
+  ws.key = key;
+  return ws.valid;
 }
 
-// processes one queued tile (whole warp)
-__device__ void process_tile(Shared& S, const Table& T, int slot, int lane) {
+// processes one queued block (whole warp)
+template <int BH>
+__device__ void process_block(Shared& S, const Table& T, int slot, int lane, WarpST& wst) {
+  using L = Lo<BH>;
   const Ctx& c = S.c;
   const uint64_t key = ldcg64(&T.keys[slot]);
-  const int tx = (int)(uint32_t)(key & 0xffffffffu);
-  const int ty = (int)(uint32_t)(key >> 32);
-  uint32_t* rec = T.recs + (size_t)slot * kRecWords;
-  double w[8];
-  bool have_w = false;
-  SuperTile st;
-  bool have_st = false;
+  const int bx = (int)(uint32_t)(key & 0xffffffffu);
+  const int by = (int)(uint32_t)(key >> 32);
+  uint32_t* rec = T.recs + (size_t)slot * T.rec_words;
   unsigned long long local_count = 0, local_eval = 0, local_fp64 = 0;
-  double local_wsum = 0.0;
+  long long local_fx = 0;  // weight sum, units of 2^-16
   uint32_t edge = 0;
+  // dequeued: queued set, busy clear -> clear queued, set busy
+  uint32_t st0 = 0;
+  if (lane == 0) {
+    st0 = atomicXor(&rec[L::kState], kQ | kB);
+    __threadfence_block();
+  }
+  st0 = __shfl_sync(0xffffffffu, st0, 0);
+  bool hdone = (st0 & kD) != 0;
+  uint32_t h_row = 0, f_cur = 0;  // lane r < BH: row r
+  if (lane < BH) {
+    f_cur = ldcg32(&rec[L::kF + lane]);
+    if (hdone) h_row = ldcg32(&rec[L::kH + lane]);
+  }
   for (int pass = 0;; pass++) {
-    if (pass > 4096) {  // a tile re-queued without end: give up on the point
+    if (lane == 0) beat(S.hb, 3, S.point, (unsigned)pass);
+    unsigned late = 0;
+    if (lane == 0) late = overdue(S, 5);
+    if (__shfl_sync(0xffffffffu, late, 0)) break;
+    if (pass > 4096) {  // a block re-queued without end: give up on the point
       if (lane == 0) {
         set_abort(S, kStTimeout);
         atomicAdd(&S.dbg_again, 1u);
-        S.dbg_state = atomicAdd(&rec[kRState], 0u);
-        S.dbg_slot = (unsigned)slot;
       }
       break;
     }
-    if (lane == 0) atomicExch(&rec[kRState], kBusy);
-    __syncwarp();
     __threadfence_block();
-    uint32_t ew = 0;
-    if (lane < 11) ew = atomicExch(&rec[lane], 0u);
-    const uint32_t ebot = __shfl_sync(0xffffffffu, ew, kRBot);
-    const uint32_t etop = __shfl_sync(0xffffffffu, ew, kRTop);
-    const uint32_t elr = __shfl_sync(0xffffffffu, ew, kRLR);
-    // this lane's row (lanes 0..7)
-    uint32_t e_row = 0;
-    if (lane < 8) {
-      e_row = ew | (lane == 0 ? ebot : 0u) | (lane == 7 ? etop : 0u) | ((elr >> lane) & 1u) |
-              (((elr >> (8 + lane)) & 1u) << 31);
+    uint32_t e_row = lane < BH ? atomicExch(&rec[lane], 0u) : 0u;
+    uint32_t eside = lane < 4 ? atomicExch(&rec[BH + lane], 0u) : 0u;
+    const uint32_t ebot = __shfl_sync(0xffffffffu, eside, 0);
+    const uint32_t etop = __shfl_sync(0xffffffffu, eside, 1);
+    const uint32_t eleft = __shfl_sync(0xffffffffu, eside, 2);
+    const uint32_t eright = __shfl_sync(0xffffffffu, eside, 3);
+    if (lane < BH) {
+      e_row |= (lane == 0 ? ebot : 0u) | (lane == BH - 1 ? etop : 0u) | ((eleft >> lane) & 1u) |
+               (((eright >> lane) & 1u) << 31);
     }
-    uint32_t Hrow[8];
-    uint32_t hdone = 0;
-    if (lane == 0) hdone = ldcg32(&rec[kRHDone]);
-    hdone = __shfl_sync(0xffffffffu, hdone, 0);
+    bool fresh = false;
+    float wall = 0.f;
     if (!hdone) {
-      unsigned nr, n64;
-      if (c.split && !have_st) have_st = get_supertile(S, T, tx, ty, lane, &st);
-      if (c.split && have_st && st.mode != kModeFp64) {
-        float wf[8];
-        eval_tile_split(c, st, tx, ty, lane, Hrow, wf, &nr, &n64);
-#pragma unroll
-        for (int r = 0; r < 8; r++) w[r] = wf[r];
+      unsigned nr = 0, n64 = 0;
+      if (lane == 0) beat(S.hb, 7, S.point, 0);
+      const long long e0 = clock64();
+      const bool have = c.split && warp_supertile<BH>(S, T, bx, by, lane, wst);
+      if (have && wst.st.mode != kModeFp64) {
+        const SuperTile stc = wst.st;  // by value: the coefficients stay in registers
+        const int K = stc.mode == kModeTaylor ? stc.K : 0;
+        if (K == 0) h_row = classify_block<BH, 0>(c, stc, bx, by, lane, &wall, &nr, &n64);
+        else if (K <= 2) h_row = classify_block<BH, 2>(c, stc, bx, by, lane, &wall, &nr, &n64);
+        else if (K <= 4) h_row = classify_block<BH, 4>(c, stc, bx, by, lane, &wall, &nr, &n64);
+        else h_row = classify_block<BH, 8>(c, stc, bx, by, lane, &wall, &nr, &n64);
       } else {
-        eval_tile_fp64(c, tx, ty, lane, Hrow, w, &nr);
-        n64 = nr;
+        h_row = classify_block_fp64<BH>(c, bx, by, lane, &wall, &nr, &n64);
       }
-      have_w = true;
+      if (S.profiling && lane == 0) atomicAdd(&S.prof[6], (unsigned long long)(clock64() - e0));
       local_eval += warp_sum_u(nr);
       local_fp64 += warp_sum_u(n64);
-      if (lane < 8) __stcg(&rec[kRH + lane], Hrow[lane]);
-      __threadfence_block();
-      if (lane == 0) __stcg(&rec[kRHDone], 1u);
-    } else {
-      uint32_t hv = lane < 8 ? ldcg32(&rec[kRH + lane]) : 0u;
-#pragma unroll
-      for (int r = 0; r < 8; r++) Hrow[r] = __shfl_sync(0xffffffffu, hv, r);
+      if (lane < BH) __stcg(&rec[L::kH + lane], h_row);
+      hdone = true;
+      fresh = true;
     }
-    uint32_t h_lane = 0;  // Hrow is uniform; lane r < 8 keeps row r
-#pragma unroll
-    for (int r = 0; r < 8; r++)
-      if (lane == r) h_lane = Hrow[r];
-    const uint32_t f_old = lane < 8 ? ldcg32(&rec[kRF + lane]) : 0u;
-    const uint32_t hp = h_lane & ~f_old;  // accepted, not yet filled
+    const uint32_t hp = h_row & ~f_cur;  // accepted, not yet filled
     uint32_t f = e_row & hp;
     if (__ballot_sync(0xffffffffu, f != 0u)) {
-      // closure inside the tile: rows exchange with the rows above/below
-      for (int it = 0; it < 64; it++) {
+      // closure inside the block: rows exchange with the rows above/below
+      // every iteration that changes anything fills at least one more run,
+      // so 32 rows x 16 runs bounds it
+      if (lane == 0) beat(S.hb, 4, S.point, 0);
+      for (int it = 0; it < 1024; it++) {
+        if ((it & 63) == 63) {
+          unsigned late = 0;
+          if (lane == 0) late = overdue(S, 6);
+          if (__shfl_sync(0xffffffffu, late, 0)) break;
+        }
         uint32_t below = __shfl_up_sync(0xffffffffu, f, 1);
         uint32_t above = __shfl_down_sync(0xffffffffu, f, 1);
         if (lane == 0) below = 0u;
-        if (lane >= 7) above = 0u;
-        uint32_t nf = lane < 8 ? run_fill(f | ((below | above) & hp), hp) : 0u;
+        if (lane >= BH - 1) above = 0u;
+        const uint32_t nf = lane < BH ? run_fill(f | ((below | above) & hp), hp) : 0u;
         const unsigned changed = __ballot_sync(0xffffffffu, nf != f);
         f = nf;
         if (!changed) break;
       }
-      if (lane < 8) __stcg(&rec[kRF + lane], f_old | f);
-      uint32_t nw[8];
-#pragma unroll
-      for (int r = 0; r < 8; r++) nw[r] = __shfl_sync(0xffffffffu, f, r);
-      // weights and count of the newly filled rays
-      double acc = 0.0;
-      unsigned cnt = 0;
-      unsigned re_eval = 0;
-      const int64_t nx = (int64_t)tx * 32 + lane;
-      if (!have_w && c.split && !have_st) have_st = get_supertile(S, T, tx, ty, lane, &st);
-#pragma unroll
-      for (int r = 0; r < 8; r++) {
-        cnt += __popc(nw[r]);
-        if ((nw[r] >> lane) & 1u) {
-          if (have_w) {
-            acc += w[r];
-          } else if (c.split && have_st && st.mode != kModeFp64) {
-            acc += (double)weight_split(c, st, nx, (int64_t)ty * 8 + r);
-            re_eval++;
-          } else {
-            const double rsq = irs_exact(c, grid_x(c, nx), grid_y(c, (int64_t)ty * 8 + r));
-            acc += ray_weight(c, rsq);
-            re_eval++;
+      const uint32_t f_new = f_cur | f;
+      if (lane < BH) __stcg(&rec[L::kF + lane], f_new);
+      const uint32_t fl = __ballot_sync(0xffffffffu, lane < BH && (f_new & 1u));
+      const uint32_t fr = __ballot_sync(0xffffffffu, lane < BH && (f_new >> 31));
+      if (lane == 0) {
+        __stcg(&rec[L::kFl], fl);
+        __stcg(&rec[L::kFr], fr);
+      }
+      // weights of the newly filled rays: the whole evaluated block when this
+      // pass filled all of its accepted rays, otherwise ray by ray
+      float acc;
+      const bool all = fresh && __ballot_sync(0xffffffffu, lane < BH && f != h_row) == 0u;
+      if (all) {
+        acc = wall;
+      } else {
+        acc = 0.f;
+        unsigned re = 0;
+        const int64_t nx = (int64_t)bx * 32 + lane;
+        if (c.split) warp_supertile<BH>(S, T, bx, by, lane, wst);
+#pragma unroll 1
+        for (int r = 0; r < BH; r++) {
+          const uint32_t nwr = __shfl_sync(0xffffffffu, f, r);
+          if ((nwr >> lane) & 1u) {
+            acc += weight_again(c, wst.st, c.split && wst.valid, nx, (int64_t)by * BH + r);
+            re++;
           }
         }
+        local_eval += warp_sum_u(re);
       }
-      acc = warp_sum(acc);
-      re_eval = warp_sum_u(re_eval);
-      local_eval += re_eval;
-      if (!c.split) local_fp64 += re_eval;
-      local_count += cnt;
-      local_wsum += acc;
+      f_cur = f_new;
+      local_count += warp_sum_u(lane < BH ? __popc(f) : 0u);
+      // a block's sum is below 1024 * 1.5: 2^-16 resolution fits an int32
+      local_fx += (long long)__float2int_rn(warp_sum_f(acc) * 65536.f);
       // plane edge: columns 1 and N-1 are where the reference's row scan
       // stops differently (lcirs.cc:413-440)
       {
-        const int64_t c0 = (int64_t)tx * 32;
+        const int64_t c0 = (int64_t)bx * 32;
         uint32_t colmask = 0;
         if (1 >= c0 && 1 < c0 + 32) colmask |= 1u << (1 - c0);
         if (c.n - 1 >= c0 && c.n - 1 < c0 + 32) colmask |= 1u << (c.n - 1 - c0);
-        uint32_t any = 0;
-#pragma unroll
-        for (int r = 0; r < 8; r++) any |= nw[r];
+        const uint32_t any = __reduce_or_sync(0xffffffffu, lane < BH ? f : 0u);
         if (any & colmask) edge = 1;
       }
       // neighbours
+      const long long p0 = clock64();
+      if (lane == 0) beat(S.hb, 5, S.point, 0);
+      const uint32_t top = __shfl_sync(0xffffffffu, f, BH - 1);
+      const uint32_t bot = __shfl_sync(0xffffffffu, f, 0);
+      const uint32_t lcol = __ballot_sync(0xffffffffu, lane < BH && (f & 1u));
+      const uint32_t rcol = __ballot_sync(0xffffffffu, lane < BH && (f >> 31));
       if (lane == 0) {
-        push(S, T, tx, ty + 1, kRBot, nw[7]);
+        push<BH>(S, T, bx, by + 1, kPushBot, 0, top);
       } else if (lane == 1) {
-        push(S, T, tx, ty - 1, kRTop, nw[0]);
+        push<BH>(S, T, bx, by - 1, kPushTop, 0, bot);
       } else if (lane == 2) {
-        uint32_t b = 0;
-#pragma unroll
-        for (int r = 0; r < 8; r++) b |= (nw[r] & 1u) << r;
-        push(S, T, tx - 1, ty, kRLR, b << 8);  // enters the left tile at its column 31
+        push<BH>(S, T, bx - 1, by, kPushRight, 0, lcol);  // enters the left block at column 31
       } else if (lane == 3) {
-        uint32_t b = 0;
-#pragma unroll
-        for (int r = 0; r < 8; r++) b |= (nw[r] >> 31) << r;
-        push(S, T, tx + 1, ty, kRLR, b);  // enters the right tile at its column 0
+        push<BH>(S, T, bx + 1, by, kPushLeft, 0, rcol);   // enters the right block at column 0
       }
       __syncwarp();
+      if (S.profiling && lane == 0) atomicAdd(&S.prof[7], (unsigned long long)(clock64() - p0));
     }
+    // release: H and F (stored by every lane) must be visible before the
+    // state says so
+    if (lane == 0) beat(S.hb, 6, S.point, 0);
     __threadfence_block();
+    __syncwarp();
     uint32_t again = 0;
-    if (lane == 0) again = atomicCAS(&rec[kRState], kBusy, 0u) != kBusy;
+    if (lane == 0) {
+      const uint32_t old = atomicCAS(&rec[L::kState], kB | (fresh ? 0u : kD), kD);
+      if (old != (kB | (fresh ? 0u : kD))) {
+        // queued again while busy (and, after a fresh evaluation, D not yet
+        // set): keep busy, clear queued, mark H done
+        atomicAnd(&rec[L::kState], ~kQ);
+        atomicOr(&rec[L::kState], kD);
+        again = 1;
+      }
+    }
     again = __shfl_sync(0xffffffffu, again, 0);
     if (!again) {
       if (lane == 0) atomicMax(&S.max_pass, (unsigned)pass);
@@ -789,8 +857,7 @@ __device__ void process_tile(Shared& S, const Table& T, int slot, int lane) {
   }
   if (lane == 0) {
     if (local_count) atomicAdd(&S.count, local_count);
-    if (local_wsum != 0.0)
-      atomicAdd(&S.wsum, (unsigned long long)(long long)llrint(local_wsum * kWsumScale));
+    if (local_fx) atomicAdd(&S.wsum, (unsigned long long)(local_fx << 16));
     atomicAdd(&S.rays_eval, local_eval);
     atomicAdd(&S.rays_fp64, local_fp64);
     if (edge) atomicOr(&S.status, kStEdge);
@@ -799,34 +866,48 @@ __device__ void process_tile(Shared& S, const Table& T, int slot, int lane) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(256)
+template <int BH>
+__global__ void __launch_bounds__(256, 2)
 fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int32_t* seeds,
-            PointOut* out, FillScratch sc, int split_mode) {
+            PointOut* out, FillScratch sc, int split_mode, const int32_t* list,
+            const unsigned* list_count) {
   __shared__ Shared S;
+  // with a point list (overflow retry) the work is list[0 .. *list_count)
+  const int nwork = list ? (int)*list_count : npoints;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const size_t cap = (size_t)1 << sc.cap_log2;
   Table T;
   T.keys = sc.keys + (size_t)blockIdx.x * cap;
-  T.recs = sc.recs + (size_t)blockIdx.x * cap * kRecWords;
+  T.recs = sc.recs + (size_t)blockIdx.x * cap * sc.rec_words;
   T.ring = sc.ring + (size_t)blockIdx.x * cap;
   T.used = sc.used + (size_t)blockIdx.x * cap;
   T.mask = (uint32_t)(cap - 1);
+  T.rec_words = sc.rec_words;
   const size_t scap = (size_t)1 << kSuperLog2;
   T.skeys = sc.skeys + (size_t)blockIdx.x * scap;
   T.sents = sc.sents + (size_t)blockIdx.x * scap * kSEntryWords;
   T.sused = sc.sused + (size_t)blockIdx.x * scap;
   T.smask = (uint32_t)(scap - 1);
+  WarpST wst;
+  wst.valid = false;
+  wst.key = 0;
 
   for (;;) {
     if (threadIdx.x == 0) {
-      S.point = (int)atomicAdd(sc.next_point, 1u);
+      {
+        const int w = (int)atomicAdd(sc.next_point, 1u);
+        S.point = w < nwork ? (list ? list[w] : w) : npoints;
+      }
       S.head = S.tail = S.pending = S.used = S.sused = 0;
       S.abort_ = 0;
       S.count = S.wsum = S.rays_eval = S.rays_fp64 = 0;
       S.status = 0;
       S.t0 = globaltimer();
-      S.dbg_again = S.dbg_state = S.dbg_slot = S.dbg_deq = S.max_pass = 0;
+      S.dbg_again = S.dbg_deq = S.max_pass = S.dbg_where = 0;
+      S.profiling = sc.prof != nullptr;
+      S.hb = sc.heartbeat;
+      for (int q = 0; q < 8; q++) S.prof[q] = 0;
       if (S.point < npoints) {
         const PointIn pi = points[S.point];
         const DevLens& D = lenses[pi.lens];
@@ -849,7 +930,7 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
         c.z3y = D.L.z3.im;
         c.binary = D.ray_binary;
         c.txmax = (int)((c.n - 1) >> 5);
-        c.tymax = (int)((c.n - 1) >> 3);
+        c.tymax = (int)((c.n - 1) / BH);
         c.split = split_mode;
         // super-tile edge: 2^9 pixels when h is small, down to 2^7 when the
         // grid is coarse (the expansion's ratio |delta|/|W| stays ~1e-3)
@@ -868,6 +949,7 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
     __syncthreads();
     const int p = S.point;
     if (p >= npoints) break;
+    wst.valid = false;
     const bool skip = (S.status & kStBadInput) != 0;
     // seeds (lcirs.cc:171-174; seed rows must satisfy 0 < ny < N, 386-391)
     if (!skip && warp == 0) {
@@ -880,15 +962,17 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
           atomicOr(&S.status, kStEdge);
           continue;
         }
-        push(S, T, sx >> 5, sy >> 3, kRSeed + (sy & 7), 1u << (sx & 31));
+        push<BH>(S, T, sx >> 5, sy / BH, kPushSeed, sy % BH, 1u << (sx & 31));
       }
     }
     __syncthreads();
     // work loop
+    const long long wl0 = clock64();
     if (!skip) {
       unsigned spins = 0;
       for (;;) {
         int slot = -1;
+        if (lane == 0) beat(S.hb, 1, p, spins);
         if (lane == 0) slot = try_dequeue(S, T);
         slot = __shfl_sync(0xffffffffu, slot, 0);
         if (slot < 0) {
@@ -899,16 +983,34 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
             if (lane == 0) set_abort(S, kStTimeout);
             break;
           }
+          if ((spins & 255) == 255) {
+            unsigned late = 0;
+            if (lane == 0) late = overdue(S, 7);
+            if (__shfl_sync(0xffffffffu, late, 0)) break;
+          }
+          if (S.profiling && lane == 0) atomicAdd(&S.prof[2], 1ull);
           __nanosleep(100);
           continue;
         }
         spins = 0;
-        if (lane == 0 && globaltimer() - S.t0 > kPointDeadlineNs) set_abort(S, kStTimeout);
-        if (!*(volatile unsigned*)&S.abort_) process_tile(S, T, slot, lane);
+        if (lane == 0) overdue(S, 8);
+        const long long c0 = clock64();
+        if (lane == 0) beat(S.hb, 2, p, (unsigned)slot);
+        if (!*(volatile unsigned*)&S.abort_) process_block<BH>(S, T, slot, lane, wst);
+        if (S.profiling && lane == 0) {
+          atomicAdd(&S.prof[0], 1ull);
+          atomicAdd(&S.prof[1], (unsigned long long)(clock64() - c0));
+        }
         if (lane == 0) atomicSub(&S.pending, 1u);
       }
     }
+    if (S.profiling && lane == 0) atomicAdd(&S.prof[3], (unsigned long long)(clock64() - wl0));
+    if (lane == 0) beat(S.hb, 8, p, 0);
     __syncthreads();
+    if (S.profiling && threadIdx.x == 0) {
+      S.prof[4] = S.sused;
+      for (int q = 0; q < 8; q++) atomicAdd(&sc.prof[q], S.prof[q]);
+    }
     if (threadIdx.x == 0) {
       PointOut o = out[p];
       o.count = S.count;
@@ -916,7 +1018,7 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
       o.status |= S.status;
       o.tiles = S.used;
       o.diag = S.max_pass | (S.dbg_again ? 0x10000u : 0u) | (S.dbg_deq ? 0x20000u : 0u) |
-              ((S.dbg_state & 0xffu) << 24);
+               (S.dbg_where << 24);
       o.rays_eval = S.rays_eval;
       o.rays_fp64 = S.rays_fp64;
       out[p] = o;
@@ -925,25 +1027,31 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
     const unsigned nused = S.used < cap ? S.used : (unsigned)cap;
     for (unsigned u = threadIdx.x; u < nused; u += blockDim.x) {
       const uint32_t slot = __ldcg(&T.used[u]);
-      if (sc.dump) {
-        uint32_t fm[8], any = 0;
-        for (int r = 0; r < 8; r++) any |= (fm[r] = ldcg32(&T.recs[(size_t)slot * kRecWords + kRF + r]));
+      uint32_t* rec = T.recs + (size_t)slot * T.rec_words;
+      if (sc.dump && !S.abort_) {  // an aborted point is retried and dumped then
+        uint32_t any = 0;
+        for (int r = 0; r < BH; r++) any |= ldcg32(&rec[Lo<BH>::kF + r]);
         if (any) {
-          const unsigned d = atomicAdd(sc.dump_count, 1u);
-          if (d < sc.dump_cap) {
-            const uint64_t key = ldcg64(&T.keys[slot]);
-            uint32_t* o = sc.dump + (size_t)d * kDumpWords;
-            o[0] = (uint32_t)p;
-            o[1] = (uint32_t)(key & 0xffffffffu);
-            o[2] = (uint32_t)(key >> 32);
-            for (int r = 0; r < 8; r++) o[3 + r] = fm[r];
+          const uint64_t key = ldcg64(&T.keys[slot]);
+          const int bxk = (int)(uint32_t)(key & 0xffffffffu), byk = (int)(uint32_t)(key >> 32);
+          for (int t8 = 0; t8 < BH / 8; t8++) {  // one record per 32x8 tile
+            uint32_t fm[8], a8 = 0;
+            for (int r = 0; r < 8; r++) a8 |= (fm[r] = ldcg32(&rec[Lo<BH>::kF + 8 * t8 + r]));
+            if (!a8) continue;
+            const unsigned d = atomicAdd(sc.dump_count, 1u);
+            if (d < sc.dump_cap) {
+              uint32_t* o = sc.dump + (size_t)d * kDumpWords;
+              o[0] = (uint32_t)p;
+              o[1] = (uint32_t)bxk;
+              o[2] = (uint32_t)(byk * (BH / 8) + t8);
+              for (int r = 0; r < 8; r++) o[3 + r] = fm[r];
+            }
           }
         }
       }
       __stcg((unsigned long long*)&T.keys[slot], (unsigned long long)kEmptyKey);
-      uint4* r4 = (uint4*)(T.recs + (size_t)slot * kRecWords);
-#pragma unroll
-      for (int q = 0; q < kRecWords / 4; q++) __stcg(&r4[q], make_uint4(0u, 0u, 0u, 0u));
+      uint4* r4 = (uint4*)rec;
+      for (int q = 0; q < T.rec_words / 4; q++) __stcg(&r4[q], make_uint4(0u, 0u, 0u, 0u));
     }
     const unsigned nsu = S.sused < scap ? S.sused : (unsigned)scap;
     for (unsigned u = threadIdx.x; u < nsu; u += blockDim.x) {
@@ -964,22 +1072,30 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
   }
 }
 
-size_t fill_scratch_bytes(int ctas, int cap_log2) {
+int block_rec_words(int bh) {
+  return bh == 8 ? Lo<8>::kWords : (bh == 16 ? Lo<16>::kWords : Lo<32>::kWords);
+}
+
+size_t fill_scratch_bytes(int ctas, int cap_log2, int bh) {
   const size_t cap = (size_t)1 << cap_log2;
   const size_t scap = (size_t)1 << kSuperLog2;
-  return (size_t)ctas * cap * (8 + kRecWords * 4 + 4 + 4) +
+  return (size_t)ctas * cap * (8 + (size_t)block_rec_words(bh) * 4 + 4 + 4) +
          (size_t)ctas * scap * (8 + kSEntryWords * 4 + 4) + 256;
 }
 
-void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, cudaStream_t st) {
+void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, int bh,
+                       cudaStream_t st) {
   const size_t cap = (size_t)1 << cap_log2;
+  const int rw = block_rec_words(bh);
   char* p = (char*)base;
   s->ctas = ctas;
   s->cap_log2 = cap_log2;
+  s->block_h = bh;
+  s->rec_words = rw;
   s->keys = (uint64_t*)p;
   p += (size_t)ctas * cap * 8;
   s->recs = (uint32_t*)p;
-  p += (size_t)ctas * cap * kRecWords * 4;
+  p += (size_t)ctas * cap * rw * 4;
   s->ring = (uint32_t*)p;
   p += (size_t)ctas * cap * 4;
   s->used = (uint32_t*)p;
@@ -995,8 +1111,10 @@ void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, cudaS
   s->dump = nullptr;
   s->dump_count = nullptr;
   s->dump_cap = 0;
+  s->prof = nullptr;
+  s->heartbeat = nullptr;
   cudaMemsetAsync(s->keys, 0xff, (size_t)ctas * cap * 8, st);
-  cudaMemsetAsync(s->recs, 0, (size_t)ctas * cap * kRecWords * 4, st);
+  cudaMemsetAsync(s->recs, 0, (size_t)ctas * cap * rw * 4, st);
   cudaMemsetAsync(s->ring, 0, (size_t)ctas * cap * 4, st);
   cudaMemsetAsync(s->skeys, 0xff, (size_t)ctas * scap * 8, st);
   cudaMemsetAsync(s->sents, 0, (size_t)ctas * scap * kSEntryWords * 4, st);
@@ -1011,12 +1129,45 @@ int fill_default_ctas() {
 
 void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                  const int32_t* d_seeds, PointOut* d_out, const FillScratch& s, int mode,
-                 int threads, cudaStream_t st) {
+                 int threads, cudaStream_t st, const int32_t* d_list, const unsigned* d_count) {
   if (npoints <= 0) return;
   cudaMemsetAsync(s.next_point, 0, sizeof(unsigned), st);
   const int ctas = s.ctas;
-  fill_kernel<<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
-                                        mode == kFillSplit ? 1 : 0);
+  const int split = mode == kFillSplit ? 1 : 0;
+  switch (s.block_h) {
+    case 8:
+      fill_kernel<8><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
+                                                 split, d_list, d_count);
+      break;
+    case 16:
+      fill_kernel<16><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
+                                                  split, d_list, d_count);
+      break;
+    default:
+      fill_kernel<32><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
+                                                  split, d_list, d_count);
+      break;
+  }
+}
+
+// Points whose block table overflowed: clear their transient status bits and
+// list them for a retry with a larger table.
+__global__ void collect_overflow_kernel(PointOut* out, int npoints, int32_t* list,
+                                        unsigned* count) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npoints) return;
+  const uint32_t st = out[p].status;
+  if (st & kStTableFull) {
+    out[p].status = st & ~(kStTableFull | kStTimeout);
+    list[atomicAdd(count, 1u)] = p;
+  }
+}
+
+void launch_collect_overflow(PointOut* d_out, int npoints, int32_t* d_list, unsigned* d_count,
+                             cudaStream_t st) {
+  if (npoints <= 0) return;
+  cudaMemsetAsync(d_count, 0, sizeof(unsigned), st);
+  collect_overflow_kernel<<<(npoints + 255) / 256, 256, 0, st>>>(d_out, npoints, d_list, d_count);
 }
 
 }  // namespace tl
