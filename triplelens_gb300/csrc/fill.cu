@@ -319,7 +319,8 @@ __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
 // is below u*rho/2; where no K qualifies, the exact difference form
 //   s = D0 + delta + sum_i m_i conj(delta / ((W_i + delta) W_i))
 // is used in FP32, and where a lens lies inside the super-tile, FP64.
-// K is rounded up to 2, 4 or 8 (three compiled variants).
+// K is rounded up to 2 or 4 (two compiled variants); super-tiles that need
+// more terms use the exact difference form in FP32.
 // From the magnitudes of the terms the super-tile also gets an error bound E
 // on s and a band B = 4 rho E + 4 E^2 + 4 u rho^2 on r^2: a ray with
 // |r^2 - rho^2| <= B is classified by the exact FP64 map (irs_exact), so the
@@ -335,7 +336,7 @@ struct SuperTile {
   int mode, K;
   int nxc, nyc;
   float d0x, d0y, band;
-  float cr[8], ci[8];   // Taylor coefficients c_1..c_K, or W_i (mode 1)
+  float cr[4], ci[4];   // Taylor coefficients c_1..c_K, or W_i (mode 1)
 };
 
 __device__ __forceinline__ double shfl_d(double v, int src) {
@@ -370,9 +371,9 @@ __device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, i
   // m_i u_i^(n+1), reduced over the three lanes
   const float fux = (float)ux, fuy = (float)uy;
   float pr = (float)(mi * ux), pi = (float)(mi * uy);   // m u^1
-  float cr[8], ci[8];
+  float cr[4], ci[4];
 #pragma unroll
-  for (int n = 0; n < 8; n++) {
+  for (int n = 0; n < 4; n++) {
     const float tr = pr * fux - pi * fuy, ti = pr * fuy + pi * fux;  // m u^(n+2)
     pr = tr;
     pi = ti;
@@ -385,13 +386,18 @@ __device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, i
   }
   // tail bounds and mode (uniform; computed from lanes 0..2)
   double qmax = 0.0, wmin = 1e300, ex1 = 0.0;
-  double tk[9];
-  for (int K = 1; K <= 8; K++) {
-    double t = 0.0;
-    if (lane < 3 && q < 1.0) t = mi * uabs * pow(q, (double)(K + 1)) / (1.0 - q);
-    else if (lane < 3) t = 1e300;
-    t += shfl_d(t, 1) + shfl_d(t, 2);
-    tk[K] = shfl_d(t, 0);
+  double tk[5];
+  {
+    const double tail0 = (lane < 3 && q < 1.0) ? mi * uabs / (1.0 - q) : 0.0;
+    double qp = q;
+    for (int K = 1; K <= 4; K++) {
+      qp *= q;   // q^(K+1)
+      double t = 0.0;
+      if (lane < 3 && q < 1.0) t = tail0 * qp;
+      else if (lane < 3) t = 1e300;
+      t += shfl_d(t, 1) + shfl_d(t, 2);
+      tk[K] = shfl_d(t, 0);
+    }
   }
   {
     double a = lane < 3 ? q : 0.0, b = lane < 3 ? wabs : 1e300;
@@ -408,12 +414,12 @@ __device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, i
   int mode = kModeFp64, K = 0;
   double E = 0.0;
   if (qmax < 0.5) {
-    for (int k = 1; k <= 8; k++)
+    for (int k = 1; k <= 4; k++)
       if (tk[k] <= 0.5 * u * c.rho) { K = k; break; }
   }
-  // three compiled orders keep the kernel's code small: round K up to 2, 4
-  // or 8 (more terms only shrink the tail)
-  if (K > 0) K = K <= 2 ? 2 : (K <= 4 ? 4 : 8);
+  // two compiled orders keep the kernel's code and registers small: round K
+  // up to 2 or 4 (more terms only shrink the tail)
+  if (K > 0) K = K <= 2 ? 2 : 4;
   if (K > 0) {
     double sc = 0.0, dp = dmax;
     for (int n = 0; n < K; n++) {
@@ -434,7 +440,7 @@ __device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, i
     __stcg(&ent[kSD0y], __float_as_uint((float)d0y));
     __stcg(&ent[kSBand], __float_as_uint((float)(band * 1.0001)));
     if (mode == kModeTaylor) {
-      for (int n = 0; n < 8; n++) {
+      for (int n = 0; n < 4; n++) {
         __stcg(&ent[kSC + 2 * n], __float_as_uint(cr[n]));
         __stcg(&ent[kSC + 2 * n + 1], __float_as_uint(ci[n]));
       }
@@ -509,7 +515,7 @@ __device__ __noinline__ bool get_supertile(Shared& S, const Table& T, int64_t nx
   st->d0y = __uint_as_float(ldcg32(&ent[kSD0y]));
   st->band = __uint_as_float(ldcg32(&ent[kSBand]));
 #pragma unroll
-  for (int n = 0; n < 8; n++) {
+  for (int n = 0; n < 4; n++) {
     st->cr[n] = __uint_as_float(ldcg32(&ent[kSC + 2 * n]));
     st->ci[n] = __uint_as_float(ldcg32(&ent[kSC + 2 * n + 1]));
   }
@@ -572,26 +578,30 @@ template <int BH, int K>
 __device__ __forceinline__ uint32_t classify_block(const Ctx& c, const SuperTile st, int bx,
                                                    int by, int lane, float* wsum, unsigned* ev,
                                                    unsigned* e64) {
+  // per-block constants kept in registers across the row loop
+  const float hf = c.hf;
+  const int64_t n = c.n;
   const int64_t nx = (int64_t)bx * 32 + lane;
-  const bool col_ok = nx >= 1 && nx <= c.n - 1;
-  const float dx = c.hf * (float)(int)(nx - st.nxc);
+  const bool col_ok = nx >= 1 && nx <= n - 1;
+  const float dx = hf * (float)(int)(nx - st.nxc);
   const float bxo = st.d0x + dx;
   const float lo = c.rho2f - st.band, hi = c.rho2f + st.band;
+  const float inv_rho2 = c.inv_rho2f, lda = c.ldaf, ldb = c.ldbf;
   const int64_t ny0 = (int64_t)by * BH;
-  const int rows_ok = (int)min((int64_t)BH, c.n - ny0);  // rows <= N-1
+  const int rows_ok = col_ok ? (int)max((int64_t)0, min((int64_t)BH, n - ny0)) : 0;  // rows <= N-1
+  const int dy0 = (int)(ny0 - st.nyc);
   uint32_t hl = 0;
   float ws = 0.f;
-  unsigned nev = 0, n64 = 0;
+  unsigned n64 = 0;
 #pragma unroll 4
   for (int r = 0; r < BH; r++) {
-    const float dy = c.hf * (float)(int)(ny0 + r - st.nyc);
+    const float dy = hf * (float)(dy0 + r);
     const float r2 = split_r2<K>(c, st, dx, bxo, dy);
     bool hit = false;
-    if (col_ok && r < rows_ok) {
-      nev++;
+    if (r < rows_ok) {
       if (r2 < lo) {
         hit = true;
-        ws += ld_weight_f(c, r2);
+        ws += fmaf(ldb, sqrtf(fmaxf(0.f, fmaf(-r2, inv_rho2, 1.f))), lda);
       } else if (r2 <= hi) {
         const double rsq = irs_exact(c, grid_x(c, nx), grid_y(c, ny0 + r));
         n64++;
@@ -603,7 +613,7 @@ __device__ __forceinline__ uint32_t classify_block(const Ctx& c, const SuperTile
     if (lane == r) hl = b;
   }
   *wsum += ws;
-  *ev += nev;
+  *ev += rows_ok;
   *e64 += n64;
   return hl;
 }
@@ -650,8 +660,7 @@ __device__ __noinline__ float weight_again(const Ctx& c, const SuperTile& st, bo
   const float bx = st.d0x + dx;
   float r2;
   if (st.mode == kModeTaylor) {
-    r2 = st.K <= 2 ? taylor_r2<2>(st, dx, bx, dy)
-                   : (st.K <= 4 ? taylor_r2<4>(st, dx, bx, dy) : taylor_r2<8>(st, dx, bx, dy));
+    r2 = st.K <= 2 ? taylor_r2<2>(st, dx, bx, dy) : taylor_r2<4>(st, dx, bx, dy);
   } else {
     r2 = exact32_r2(c, st, dx, bx, dy);
   }
@@ -737,8 +746,7 @@ __device__ void process_block(Shared& S, const Table& T, int slot, int lane, War
         const int K = stc.mode == kModeTaylor ? stc.K : 0;
         if (K == 0) h_row = classify_block<BH, 0>(c, stc, bx, by, lane, &wall, &nr, &n64);
         else if (K <= 2) h_row = classify_block<BH, 2>(c, stc, bx, by, lane, &wall, &nr, &n64);
-        else if (K <= 4) h_row = classify_block<BH, 4>(c, stc, bx, by, lane, &wall, &nr, &n64);
-        else h_row = classify_block<BH, 8>(c, stc, bx, by, lane, &wall, &nr, &n64);
+        else h_row = classify_block<BH, 4>(c, stc, bx, by, lane, &wall, &nr, &n64);
       } else {
         h_row = classify_block_fp64<BH>(c, bx, by, lane, &wall, &nr, &n64);
       }
