@@ -104,6 +104,45 @@ void lcirs_set_precision(LightCurveIRS* lc, int mode);
  * bit 17 dequeue limit reached, bits 24-31 the tile state seen then. */
 void lcirs_copy_diag(LightCurveIRS* lc, uint32_t* diag);
 
+/* No counterpart in the reference.  Fill-only run that allocates no device
+ * memory, for callers that cannot call cudaMalloc when they compute
+ * magnifications: programs that hand the GPU's memory to their own pool at
+ * start-up (a later cudaMalloc fails or escapes their accounting), and
+ * latency-bound loops that cannot take the device-wide synchronisation of
+ * cudaFree (often of cudaMalloc too).  The other entry points grow their
+ * buffers with cudaMalloc on demand.
+ *
+ * Same work as lcirs_fill_from_seeds for explicit source positions, on
+ * DEVICE arrays of the caller: src_xy (npoints x 2 doubles), seeds
+ * (npoints x 64 x 2 int32, the layout of lcirs_copy_seeds), nseeds (npoints
+ * int32); outputs mag (npoints doubles), and optionally counts (uint64) and
+ * status (uint32, bits as lcirs_last_status).  The object's lens, grid,
+ * limb darkening and precision are used; the current device must be the one
+ * the object was created on.  Work is queued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and the call returns without waiting.
+ *
+ * Scratch memory is one static device array of 80 MiB, held by every GPU
+ * that loads the library's device code until the process exits.  The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array and each call clears what must start at zero,
+ * so calls whose GPU work overlaps (different streams, or several host
+ * threads without ordering) race: order them on one stream.
+ *
+ * Limits: at most LCIRS_NOALLOC_MAX_POINTS points per call (larger calls
+ * return -3 and print the limit to stderr, nothing runs), and per point a
+ * table of 16384 blocks of 32 x 32 rays (3/4 usable: magnifications up to
+ * ~100 at 200 rays per source radius, ~15 at 500); a point whose images need
+ * more gets status bit 4 and an incomplete magnification (the allocating
+ * entry points retry it with larger tables).
+ *
+ * Returns 0 when the work was queued, -1 bad argument, -2 CUDA error,
+ * -3 too many points. */
+#define LCIRS_NOALLOC_MAX_POINTS 8192
+int lcirs_fill_device_noalloc(LightCurveIRS* lc, int npoints, const double* src_xy,
+                              const int32_t* seeds, const int32_t* nseeds, double* mag,
+                              uint64_t* counts, uint32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

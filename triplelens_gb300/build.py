@@ -30,11 +30,13 @@ UNITS = [
     ("engine_host.cu", []),
     ("lcirs_abi.cu", []),
     ("batch_abi.cu", []),
+    ("noalloc_abi.cu", []),
     ("ccc_abi.cu", ["--fmad=false"]),
 ]
 
 LIBS = {
-    "liblcirs.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu"],
+    "liblcirs.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
+                    "noalloc_abi.cu"],
     "libccc.so": ["seeds.cu", "engine_host.cu", "fill.cu", "ccc_abi.cu"],
 }
 

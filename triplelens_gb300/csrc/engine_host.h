@@ -11,6 +11,8 @@
 
 #include "engine.h"
 
+struct LightCurveIRS;
+
 namespace tl {
 
 struct DevBuf {
@@ -29,6 +31,9 @@ struct Run {
   unsigned* dump_count;
   unsigned dump_cap;
 };
+
+// device copy of an object's lens, grid and limb darkening (lcirs_abi.cu)
+const DevLens* object_device_lens(const LightCurveIRS* lc);
 
 class Engine {
  public:

@@ -347,6 +347,10 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
 // ---------------------------------------------------------------------------
 // C ABI (src/LightCurves/lcirs.cc:515-609 and additive entry points)
 // ---------------------------------------------------------------------------
+namespace tl {
+const DevLens* object_device_lens(const LightCurveIRS* lc) { return lc->impl->d_lens; }
+}  // namespace tl
+
 extern "C" {
 
 LightCurveIRS* lcirs_new(double a, double b, double th, double m2, double m3, double sourceSize,
