@@ -1,0 +1,72 @@
+"""C ABI of bin/liblcirs.so without a GPU: the library builds (nvcc cross-
+compiles for sm_103a), loads, and exports every function that include/*.h
+declares; the reference's six ctypes entry points (src/LightCurves/lcirs.cc:
+515-609, bound by Examples/ctypes_classes.py:128-193) are among them.  No
+entry point is called here (every one of them reaches the GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+
+REFERENCE_ABI = ["lcirs_new", "get_lc", "get_lc_irs", "copy_lc", "set_limb_darkening",
+                 "set_amoeba_printout"]
+
+
+def declared_functions(path):
+    """Names of the functions declared in a C header (comments and
+    preprocessor lines removed; one declaration per ';')."""
+    with open(path) as f:
+        src = f.read()
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", " ", src)
+    src = "\n".join(l for l in src.splitlines() if not l.lstrip().startswith("#"))
+    src = src.replace('extern "C" {', " ").replace("}", " ")
+    names = []
+    for stmt in src.split(";"):
+        stmt = " ".join(stmt.split())
+        if "(" not in stmt or stmt.startswith("typedef"):
+            continue
+        m = re.match(r"^[\w\s\*]+?\b(\w+)\s*\(", stmt)
+        if m:
+            names.append(m.group(1))
+    return names
+
+
+def c_headers():
+    return sorted(os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h"))
+
+
+def test_headers_declare_the_reference_abi():
+    names = set()
+    for h in c_headers():
+        names.update(declared_functions(h))
+    for n in REFERENCE_ABI:
+        assert n in names
+    assert len(names) >= len(REFERENCE_ABI) + 10
+
+
+@pytest.mark.parametrize("header", [os.path.basename(h) for h in c_headers()])
+def test_library_exports_every_declared_function(product_lib, header):
+    lib = ctypes.CDLL(product_lib)
+    names = declared_functions(os.path.join(INCLUDE, header))
+    assert names, header
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, "%s declares functions the library does not export: %s" % (header,
+                                                                                     missing)
+
+
+def test_product_path_has_no_oracle_dependency():
+    """The shipped package never imports the oracle (it is test
+    infrastructure)."""
+    pkg = os.path.join(ROOT, "triplelens_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".h", ".cpp")):
+                with open(os.path.join(dirpath, f)) as fh:
+                    text = fh.read()
+                assert "import oracle" not in text and "from oracle" not in text, f
+                assert "liboracle" not in text, f
