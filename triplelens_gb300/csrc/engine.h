@@ -160,6 +160,8 @@ constexpr int kFillLevels = 3;
 constexpr int kFillLevelCtas[kFillLevels] = {0, 64, 16};
 constexpr int kFillLevelLog2[kFillLevels] = {17, 20, 22};
 
-int fill_default_ctas();
+int fill_default_ctas();        // SMs x fill_occupancy()
+void set_fill_occupancy(int occ);  // 2, 3 or 4 resident fill CTAs per SM
+int fill_occupancy();
 
 }  // namespace tl

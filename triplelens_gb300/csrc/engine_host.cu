@@ -50,6 +50,7 @@ Engine::Engine() {
     sync_steps = atoi(c) >= 2;
   }
   if (const char* c = getenv("TL_FILL_CTAS")) want_ctas_ = atoi(c);
+  if (const char* c = getenv("TL_FILL_OCC")) set_fill_occupancy(atoi(c));
   // TL_FILL_LEVELS=1 disables the overflow retries (and their tables)
   if (const char* c = getenv("TL_FILL_LEVELS")) levels_ = atoi(c);
   if (const char* c = getenv("TL_FILL_PROFILE")) profiling = atoi(c) != 0;

@@ -567,13 +567,24 @@ __device__ __forceinline__ float split_r2(const Ctx& c, const SuperTile& st, flo
   return taylor_r2<(K > 0 ? K : 1)>(st, dx, bx, dy);
 }
 
+// single-instruction square root (relative error ~2^-22; weights only)
+__device__ __forceinline__ float sqrt_fast(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ float ld_weight_f(const Ctx& c, float r2) {
-  return fmaf(c.ldbf, sqrtf(fmaxf(0.f, fmaf(-r2, c.inv_rho2f, 1.f))), c.ldaf);
+  return fmaf(c.ldbf, sqrt_fast(fmaxf(0.f, fmaf(-r2, c.inv_rho2f, 1.f))), c.ldaf);
 }
 
 // Rays of this lane's column in block (bx, by), split-precision map with the
 // FP64 guard band.  Returns the accepted mask of row `lane` (lane < BH) and
 // adds the weights of this lane's accepted rays to *wsum.
+// The FP32 pass is branch-free: eight independent rows per iteration, hits
+// and guard-band rays collected as per-lane column masks; the rare band rays
+// are decided in FP64 afterwards, and 32 ballots turn the column masks into
+// row masks.
 template <int BH, int K>
 __device__ __forceinline__ uint32_t classify_block(const Ctx& c, const SuperTile st, int bx,
                                                    int by, int lane, float* wsum, unsigned* ev,
@@ -590,26 +601,39 @@ __device__ __forceinline__ uint32_t classify_block(const Ctx& c, const SuperTile
   const int64_t ny0 = (int64_t)by * BH;
   const int rows_ok = col_ok ? (int)max((int64_t)0, min((int64_t)BH, n - ny0)) : 0;  // rows <= N-1
   const int dy0 = (int)(ny0 - st.nyc);
-  uint32_t hl = 0;
+  uint32_t hitm = 0, bandm = 0;
   float ws = 0.f;
-  unsigned n64 = 0;
-#pragma unroll 4
-  for (int r = 0; r < BH; r++) {
-    const float dy = hf * (float)(dy0 + r);
-    const float r2 = split_r2<K>(c, st, dx, bxo, dy);
-    bool hit = false;
-    if (r < rows_ok) {
-      if (r2 < lo) {
-        hit = true;
-        ws += fmaf(ldb, sqrtf(fmaxf(0.f, fmaf(-r2, inv_rho2, 1.f))), lda);
-      } else if (r2 <= hi) {
-        const double rsq = irs_exact(c, grid_x(c, nx), grid_y(c, ny0 + r));
-        n64++;
-        hit = rsq < c.rho2;
-        if (hit) ws += (float)ray_weight(c, rsq);
-      }
+#pragma unroll 1
+  for (int r0 = 0; r0 < BH; r0 += 8) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int r = r0 + q;
+      const float dy = hf * (float)(dy0 + r);
+      const float r2 = split_r2<K>(c, st, dx, bxo, dy);
+      const bool ok = r < rows_ok;
+      const bool hit = ok && r2 < lo;
+      const bool band = ok && r2 >= lo && r2 <= hi;
+      const float w = fmaf(ldb, sqrt_fast(fmaxf(0.f, fmaf(-r2, inv_rho2, 1.f))), lda);
+      ws += hit ? w : 0.f;
+      hitm |= (uint32_t)hit << r;
+      bandm |= (uint32_t)band << r;
     }
-    const uint32_t b = __ballot_sync(0xffffffffu, hit);
+  }
+  unsigned n64 = 0;
+  while (bandm) {  // rays within the guard band of the limb: FP64
+    const int r = __ffs(bandm) - 1;
+    bandm &= bandm - 1u;
+    const double rsq = irs_exact(c, grid_x(c, nx), grid_y(c, ny0 + r));
+    n64++;
+    if (rsq < c.rho2) {
+      hitm |= 1u << r;
+      ws += (float)ray_weight(c, rsq);
+    }
+  }
+  uint32_t hl = 0;
+#pragma unroll
+  for (int r = 0; r < BH; r++) {
+    const uint32_t b = __ballot_sync(0xffffffffu, (hitm >> r) & 1u);
     if (lane == r) hl = b;
   }
   *wsum += ws;
@@ -874,8 +898,9 @@ __device__ void process_block(Shared& S, const Table& T, int slot, int lane, War
 
 }  // namespace
 
-template <int BH>
-__global__ void __launch_bounds__(256, 2)
+// MINB: resident CTAs per SM the register budget is cut for (2, 3 or 4)
+template <int BH, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int32_t* seeds,
             PointOut* out, FillScratch sc, int split_mode, const int32_t* list,
             const unsigned* list_count) {
@@ -1128,11 +1153,21 @@ void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, int b
   cudaMemsetAsync(s->sents, 0, (size_t)ctas * scap * kSEntryWords * 4, st);
 }
 
+namespace {
+int g_fill_occ = 4;   // resident fill CTAs per SM (measured: 2 -> 56k, 3 -> 63k, 4 -> 64.5k points/s)
+}  // namespace
+
+void set_fill_occupancy(int occ) {
+  if (occ >= 2 && occ <= 4) g_fill_occ = occ;
+}
+
+int fill_occupancy() { return g_fill_occ; }
+
 int fill_default_ctas() {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return sms > 0 ? sms * 2 : 2;
+  return sms > 0 ? sms * g_fill_occ : 2;
 }
 
 void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
@@ -1144,16 +1179,23 @@ void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
   const int split = mode == kFillSplit ? 1 : 0;
   switch (s.block_h) {
     case 8:
-      fill_kernel<8><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
+      fill_kernel<8, 2><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
                                                  split, d_list, d_count);
       break;
     case 16:
-      fill_kernel<16><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
+      fill_kernel<16, 2><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
                                                   split, d_list, d_count);
       break;
     default:
-      fill_kernel<32><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
-                                                  split, d_list, d_count);
+      if (g_fill_occ == 4)
+        fill_kernel<32, 4><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out,
+                                                     s, split, d_list, d_count);
+      else if (g_fill_occ == 3)
+        fill_kernel<32, 3><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out,
+                                                     s, split, d_list, d_count);
+      else
+        fill_kernel<32, 2><<<ctas, threads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out,
+                                                     s, split, d_list, d_count);
       break;
   }
 }
