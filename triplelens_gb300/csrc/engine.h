@@ -75,7 +75,7 @@ struct SeedJob {
 struct PointIn {
   double sx, sy;
   int32_t lens;
-  int32_t pad;
+  uint32_t est_blocks;     // predicted rays / 1024 (point-source magnification)
 };
 
 struct PointOut {
@@ -116,9 +116,14 @@ struct FillScratch {
   uint64_t* skeys;         // [ctas << kSuperLog2]
   uint32_t* sents;         // [ctas << kSuperLog2][32 words]
   uint32_t* sused;         // [ctas << kSuperLog2]
-  unsigned* next_point;    // work counter (1 word)
+  unsigned* next_point;    // work counters: [0] the point list, [1] its large-point head
   int ctas;
   int cap_log2;
+  // the first big_ctas CTAs own tables of 2^big_log2 blocks and take the
+  // head of a size-ordered point list (its first *nbig entries) first
+  int big_ctas;
+  int big_log2;
+  const unsigned* nbig;
   int block_h;             // rows per block (8, 16 or 32)
   int rec_words;           // 32-bit words per block record
   // optional export of the filled masks: records of kDumpWords words
@@ -138,9 +143,16 @@ constexpr int kDumpWords = 11;
 constexpr int kSuperLog2 = 12;   // super-tile table capacity per CTA (entries)
 
 int block_rec_words(int bh);
-size_t fill_scratch_bytes(int ctas, int cap_log2, int bh);
+size_t fill_scratch_bytes(int ctas, int cap_log2, int bh, int big_ctas = 0, int big_log2 = 0);
 void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, int bh,
-                       cudaStream_t st);
+                       cudaStream_t st, int big_ctas = 0, int big_log2 = 0);
+
+// Size-ordered work list for the fill: points by decreasing predicted size
+// (PointIn::est_blocks, from the point-source magnification).  meta[0] =
+// number of points, meta[1] = number of points predicted at or above
+// big_units blocks of 1024 rays (the list's head); meta needs 2 + 2*64 words.
+void launch_order(const PointIn* d_points, int npoints, int32_t* d_list, unsigned* d_meta,
+                  unsigned big_units, cudaStream_t st);
 
 enum FillMode : int { kFillFp64 = 0, kFillSplit = 1 };
 

@@ -51,6 +51,8 @@ Engine::Engine() {
   }
   if (const char* c = getenv("TL_FILL_CTAS")) want_ctas_ = atoi(c);
   if (const char* c = getenv("TL_FILL_OCC")) set_fill_occupancy(atoi(c));
+  // TL_FILL_BIG: CTAs with the large level-0 tables (0: none)
+  if (const char* c = getenv("TL_FILL_BIG")) want_big_ctas_ = atoi(c);
   // TL_FILL_LEVELS=1 disables the overflow retries (and their tables)
   if (const char* c = getenv("TL_FILL_LEVELS")) levels_ = atoi(c);
   if (const char* c = getenv("TL_FILL_PROFILE")) profiling = atoi(c) != 0;
@@ -108,9 +110,20 @@ bool Engine::ensure_fill_scratch(int level) {
   }
   // capacities are counted in 32x8 tiles; a block holds block_h/8 of them
   for (int b = block_h_; b > 8; b >>= 1) cap--;
-  const size_t bytes = fill_scratch_bytes(ctas, cap, block_h_);
+  // level 0: the first CTAs own 4x larger tables and take the points
+  // predicted largest (those that would overflow the others' tables)
+  int big = 0, big_log2 = cap;
+  if (level == 0) {
+    big = want_big_ctas_ >= 0 ? want_big_ctas_ : (ctas >= 256 ? 64 : ctas / 4);
+    big = big > ctas ? ctas : big;
+    big_log2 = cap + 2;
+    // predicted size (units of 1024 rays) from which a point goes to them:
+    // 0.6 of the usable 3/4 of a regular table
+    big_units_ = (unsigned)(0.45 * (double)((size_t)1 << cap) * block_h_ / 32.0);
+  }
+  const size_t bytes = fill_scratch_bytes(ctas, cap, block_h_, big, big_log2);
   if (!check(cudaMalloc(&fill_base_[level], bytes))) return false;
-  fill_scratch_init(&fs_[level], fill_base_[level], ctas, cap, block_h_, stream);
+  fill_scratch_init(&fs_[level], fill_base_[level], ctas, cap, block_h_, stream, big, big_log2);
   check(cudaStreamSynchronize(stream));
   return true;
 }
@@ -144,6 +157,12 @@ void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
 void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
   if (!ensure_fill_scratch(0)) return;
   FillScratch s = fs_[0];
+  // largest points first; the head of the list goes to the large tables
+  char* ob = (char*)order_.need(sizeof(int32_t) * np + 1024);
+  unsigned* order_meta = (unsigned*)ob;
+  int32_t* order_list = (int32_t*)(ob + 1024);
+  launch_order(R.points, (int)np, order_list, order_meta, big_units_, st);
+  s.nbig = order_meta + 1;
   s.dump = R.dump;
   s.dump_count = R.dump_count;
   s.dump_cap = R.dump_cap;
@@ -159,7 +178,8 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     cudaHostGetDevicePointer((void**)&heartbeat_dev_, heartbeat_host_, 0);
   }
   s.heartbeat = heartbeat_dev_;
-  launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st);
+  launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st, order_list,
+              order_meta);
   if (heartbeat_host_) {
     // a side thread reports the warps' phases while the stream is busy; the
     // caller keeps blocking as usual

@@ -64,7 +64,9 @@ class Engine {
  private:
   Engine();
   bool ensure_fill_scratch(int level);
-  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_;
+  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_;
+  int want_big_ctas_ = -1;   // -1: 64 when there are >= 256 CTAs, else a quarter
+  unsigned big_units_ = 0;
   void* fill_base_[kFillLevels] = {nullptr, nullptr, nullptr};
   FillScratch fs_[kFillLevels]{};
   int want_ctas_ = 0, want_cap_log2_ = 17, threads_ = 256;

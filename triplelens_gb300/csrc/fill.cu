@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "engine.h"
 
 namespace tl {
@@ -909,12 +911,20 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
   const int nwork = list ? (int)*list_count : npoints;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const size_t cap = (size_t)1 << sc.cap_log2;
+  // table of this CTA: the first big_ctas CTAs own the larger tables
+  const bool big_cta = (int)blockIdx.x < sc.big_ctas;
+  const size_t cap = (size_t)1 << (big_cta ? sc.big_log2 : sc.cap_log2);
+  const size_t tbase = big_cta ? (size_t)blockIdx.x * cap
+                               : ((size_t)sc.big_ctas << sc.big_log2) +
+                                     (size_t)(blockIdx.x - sc.big_ctas) * cap;
+  const int nbig = (list && sc.nbig && big_cta) ? (int)*sc.nbig : 0;
+  const int nbig_all = (list && sc.nbig && sc.big_ctas > 0) ? (int)*sc.nbig : 0;
+  bool big_left = nbig > 0;
   Table T;
-  T.keys = sc.keys + (size_t)blockIdx.x * cap;
-  T.recs = sc.recs + (size_t)blockIdx.x * cap * sc.rec_words;
-  T.ring = sc.ring + (size_t)blockIdx.x * cap;
-  T.used = sc.used + (size_t)blockIdx.x * cap;
+  T.keys = sc.keys + tbase;
+  T.recs = sc.recs + tbase * sc.rec_words;
+  T.ring = sc.ring + tbase;
+  T.used = sc.used + tbase;
   T.mask = (uint32_t)(cap - 1);
   T.rec_words = sc.rec_words;
   const size_t scap = (size_t)1 << kSuperLog2;
@@ -929,7 +939,17 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
   for (;;) {
     if (threadIdx.x == 0) {
       {
-        const int w = (int)atomicAdd(sc.next_point, 1u);
+        // large CTAs drain the list's head (largest points) first; all CTAs
+        // then share the rest, largest first
+        int w = -1;
+        if (big_left) {
+          w = (int)atomicAdd(&sc.next_point[1], 1u);
+          if (w >= nbig) {
+            big_left = false;
+            w = -1;
+          }
+        }
+        if (w < 0) w = nbig_all + (int)atomicAdd(&sc.next_point[0], 1u);
         S.point = w < nwork ? (list ? list[w] : w) : npoints;
       }
       S.head = S.tail = S.pending = S.used = S.sused = 0;
@@ -1109,30 +1129,42 @@ int block_rec_words(int bh) {
   return bh == 8 ? Lo<8>::kWords : (bh == 16 ? Lo<16>::kWords : Lo<32>::kWords);
 }
 
-size_t fill_scratch_bytes(int ctas, int cap_log2, int bh) {
-  const size_t cap = (size_t)1 << cap_log2;
+namespace {
+// block-table entries over all CTAs
+size_t table_entries(int ctas, int cap_log2, int big_ctas, int big_log2) {
+  big_ctas = big_ctas < 0 ? 0 : (big_ctas > ctas ? ctas : big_ctas);
+  return ((size_t)big_ctas << big_log2) + ((size_t)(ctas - big_ctas) << cap_log2);
+}
+}  // namespace
+
+size_t fill_scratch_bytes(int ctas, int cap_log2, int bh, int big_ctas, int big_log2) {
+  const size_t ent = table_entries(ctas, cap_log2, big_ctas, big_log2);
   const size_t scap = (size_t)1 << kSuperLog2;
-  return (size_t)ctas * cap * (8 + (size_t)block_rec_words(bh) * 4 + 4 + 4) +
+  return ent * (8 + (size_t)block_rec_words(bh) * 4 + 4 + 4) +
          (size_t)ctas * scap * (8 + kSEntryWords * 4 + 4) + 256;
 }
 
 void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, int bh,
-                       cudaStream_t st) {
-  const size_t cap = (size_t)1 << cap_log2;
+                       cudaStream_t st, int big_ctas, int big_log2) {
+  big_ctas = big_ctas < 0 ? 0 : (big_ctas > ctas ? ctas : big_ctas);
+  const size_t ent = table_entries(ctas, cap_log2, big_ctas, big_log2);
   const int rw = block_rec_words(bh);
   char* p = (char*)base;
   s->ctas = ctas;
   s->cap_log2 = cap_log2;
+  s->big_ctas = big_ctas;
+  s->big_log2 = big_ctas > 0 ? big_log2 : cap_log2;
+  s->nbig = nullptr;
   s->block_h = bh;
   s->rec_words = rw;
   s->keys = (uint64_t*)p;
-  p += (size_t)ctas * cap * 8;
+  p += ent * 8;
   s->recs = (uint32_t*)p;
-  p += (size_t)ctas * cap * rw * 4;
+  p += ent * rw * 4;
   s->ring = (uint32_t*)p;
-  p += (size_t)ctas * cap * 4;
+  p += ent * 4;
   s->used = (uint32_t*)p;
-  p += (size_t)ctas * cap * 4;
+  p += ent * 4;
   const size_t scap = (size_t)1 << kSuperLog2;
   s->skeys = (uint64_t*)p;
   p += (size_t)ctas * scap * 8;
@@ -1146,9 +1178,9 @@ void fill_scratch_init(FillScratch* s, void* base, int ctas, int cap_log2, int b
   s->dump_cap = 0;
   s->prof = nullptr;
   s->heartbeat = nullptr;
-  cudaMemsetAsync(s->keys, 0xff, (size_t)ctas * cap * 8, st);
-  cudaMemsetAsync(s->recs, 0, (size_t)ctas * cap * rw * 4, st);
-  cudaMemsetAsync(s->ring, 0, (size_t)ctas * cap * 4, st);
+  cudaMemsetAsync(s->keys, 0xff, ent * 8, st);
+  cudaMemsetAsync(s->recs, 0, ent * rw * 4, st);
+  cudaMemsetAsync(s->ring, 0, ent * 4, st);
   cudaMemsetAsync(s->skeys, 0xff, (size_t)ctas * scap * 8, st);
   cudaMemsetAsync(s->sents, 0, (size_t)ctas * scap * kSEntryWords * 4, st);
 }
@@ -1174,7 +1206,7 @@ void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                  const int32_t* d_seeds, PointOut* d_out, const FillScratch& s, int mode,
                  int threads, cudaStream_t st, const int32_t* d_list, const unsigned* d_count) {
   if (npoints <= 0) return;
-  cudaMemsetAsync(s.next_point, 0, sizeof(unsigned), st);
+  cudaMemsetAsync(s.next_point, 0, 2 * sizeof(unsigned), st);
   const int ctas = s.ctas;
   const int split = mode == kFillSplit ? 1 : 0;
   switch (s.block_h) {
@@ -1198,6 +1230,66 @@ void launch_fill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                                                      s, split, d_list, d_count);
       break;
   }
+}
+
+// ---------------------------------------------------------------------------
+// size-ordered work list (counting sort on half-octave buckets of the
+// predicted size, largest first)
+// ---------------------------------------------------------------------------
+constexpr int kOrderBuckets = 64;
+
+__device__ __forceinline__ int order_bucket(uint32_t est) {
+  const int b = (int)(2.f * __log2f((float)est + 1.f));
+  return b < 0 ? 0 : (b >= kOrderBuckets ? kOrderBuckets - 1 : b);
+}
+
+int order_bucket_host(unsigned est) {
+  const int b = (int)(2.0 * std::log2((double)est + 1.0));
+  return b < 0 ? 0 : (b >= kOrderBuckets ? kOrderBuckets - 1 : b);
+}
+
+__global__ void order_hist_kernel(const PointIn* pts, int n, unsigned* hist) {
+  __shared__ unsigned h[kOrderBuckets];
+  if (threadIdx.x < kOrderBuckets) h[threadIdx.x] = 0;
+  __syncthreads();
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+    atomicAdd(&h[order_bucket(pts[p].est_blocks)], 1u);
+  __syncthreads();
+  if (threadIdx.x < kOrderBuckets && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+// meta: [0] points, [1] list head (buckets >= big_bucket), [2..66) histogram,
+// [66..130) cursors
+__global__ void order_scan_kernel(int n, unsigned* meta, int big_bucket) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned* hist = meta + 2;
+  unsigned* cur = meta + 2 + kOrderBuckets;
+  unsigned acc = 0, head = 0;
+  for (int b = kOrderBuckets - 1; b >= 0; b--) {
+    cur[b] = acc;
+    acc += hist[b];
+    if (b >= big_bucket) head = acc;
+  }
+  meta[0] = (unsigned)n;
+  meta[1] = head;
+}
+
+__global__ void order_scatter_kernel(const PointIn* pts, int n, unsigned* meta, int32_t* list) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const unsigned pos = atomicAdd(&meta[2 + kOrderBuckets + order_bucket(pts[p].est_blocks)], 1u);
+  if (pos < (unsigned)n) list[pos] = p;
+}
+
+void launch_order(const PointIn* d_points, int npoints, int32_t* d_list, unsigned* d_meta,
+                  unsigned big_units, cudaStream_t st) {
+  cudaMemsetAsync(d_meta, 0, sizeof(unsigned) * (2 + 2 * kOrderBuckets), st);
+  if (npoints <= 0) return;
+  const int blocks = (npoints + 255) / 256;
+  order_hist_kernel<<<blocks < 1024 ? blocks : 1024, 256, 0, st>>>(d_points, npoints,
+                                                                  d_meta + 2);
+  order_scan_kernel<<<1, 32, 0, st>>>(npoints, d_meta, order_bucket_host(big_units));
+  order_scatter_kernel<<<blocks, 256, 0, st>>>(d_points, npoints, d_meta, d_list);
 }
 
 // Points whose block table overflowed: clear their transient status bits and

@@ -92,7 +92,7 @@ __global__ void noalloc_pack_kernel(int npoints, const double* xy, const int32_t
   p.sx = x;
   p.sy = y;
   p.lens = 0;
-  p.pad = 0;
+  p.est_blocks = 0;
   points[i] = p;
   tl::PointOut o;
   o.count = 0;

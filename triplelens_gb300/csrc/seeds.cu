@@ -243,12 +243,19 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
       pi.sx = pos.re;
       pi.sy = pos.im;
       pi.lens = T.lens;
-      pi.pad = 0;
+      pi.est_blocks = 0;
       points[p] = pi;
       if (!status) {
         int n = chain_images(L, &ch, pos, imgs, &c_trig);
         if (wrong_count(L, n)) status |= kStImageCount;
         emit_seeds(g, imgs, n, seeds, &nseed, &status);
+        // predicted fill size, for the fill's largest-first order: the
+        // point-source magnification tracks the finite-source one closely
+        // (rays ~ A pi ppr^2), plus the boundary blocks
+        double a = 0.0;
+        for (int k = 0; k < n; k++) a += image_amp(L, imgs[k]);
+        const double est = a * 3.14159265358979 * (double)D.ppr * (double)D.ppr / 1024.0 * 1.15;
+        points[p].est_blocks = (uint32_t)fmin(fmax(est, 0.0), 4.0e9);
       }
     }
     status = __shfl_sync(0xffffffffu, status, 0);
