@@ -20,7 +20,7 @@ struct tl_batch {
   int ntraj = 0;
   long npoints = 0;
   int njobs = 0;
-  tl::DevBuf trajs, jobs, points, seeds, out, amp;
+  tl::DevBuf trajs, jobs, points, seeds, out, amp, trials;
   std::vector<tl::Traj> htraj;
   int precision = 1;
   uint64_t stats[4] = {0, 0, 0, 0};
@@ -44,7 +44,7 @@ tl_batch* tlb_new(void) {
 void tlb_delete(tl_batch* b) {
   if (!b) return;
   for (tl::DevBuf* d : {&b->specs, &b->lenses, &b->cc, &b->ca, &b->trajs, &b->jobs, &b->points,
-                        &b->seeds, &b->out, &b->amp})
+                        &b->seeds, &b->out, &b->amp, &b->trials})
     if (d->p) cudaFree(d->p);
   delete b;
 }
@@ -126,7 +126,8 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
   void* dp = b->points.need(sizeof(tl::PointIn) * base);
   void* dsd = b->seeds.need(sizeof(int32_t) * 2 * tl::kMaxSeeds * base);
   void* dout = b->out.need(sizeof(tl::PointOut) * base);
-  if (!dt || !dj || !dp || !dsd || !dout) return -2;
+  void* dtr = b->trials.need(sizeof(tl::TrialList) * base);
+  if (!dt || !dj || !dp || !dsd || !dout || !dtr) return -2;
   E.check(cudaMemcpyAsync(dt, b->htraj.data(), sizeof(tl::Traj) * ntraj, cudaMemcpyHostToDevice,
                           E.stream));
   E.check(cudaMemcpyAsync(dj, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
@@ -143,7 +144,8 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
   if (phase & 1)
     tl::launch_seeds((const tl::SeedJob*)b->jobs.p, b->njobs, (const tl::Traj*)b->trajs.p,
                      (const tl::DevLens*)b->lenses.p, (const cx*)b->ca.p, (tl::PointIn*)b->points.p,
-                     (int32_t*)b->seeds.p, (tl::PointOut*)b->out.p, st);
+                     (int32_t*)b->seeds.p, (tl::PointOut*)b->out.p, (tl::TrialList*)b->trials.p,
+                     st);
   if (phase & 2) {
     tl::Run R;
     R.trajs = (tl::Traj*)b->trajs.p;
@@ -151,6 +153,7 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
     R.points = (tl::PointIn*)b->points.p;
     R.seeds = (int32_t*)b->seeds.p;
     R.out = (tl::PointOut*)b->out.p;
+    R.trials = (tl::TrialList*)b->trials.p;
     R.dump = nullptr;
     R.dump_count = nullptr;
     R.dump_cap = 0;

@@ -19,7 +19,7 @@
 namespace tl {
 
 constexpr int kMaxSeeds = 64;     // seed pixels kept per point
-constexpr int kChainChunk = 16;   // points per warm-start chain (seed kernel)
+constexpr int kChainChunk = 8;    // points per warm-start chain (seed kernel)
 
 // status bits of a point (PointOut::status)
 enum : uint32_t {
@@ -100,9 +100,21 @@ void upload_trig_tables();  // Laguerre kick table + phase samples, once per dev
 void launch_lens_setup(const LensSpec* d_specs, int nlens, DevLens* d_lenses, cx* d_cc,
                        cx* d_ca, cudaStream_t st);
 
+// caustic-crossing trial points of one point, in the reference's order
+// (branch, then segment); n counts every run start, the first kMaxTrials are kept
+constexpr int kMaxTrials = 16;
+struct TrialList {
+  uint32_t n;
+  uint32_t pad;
+  cx t[kMaxTrials];
+};
+
+// seeds of every point: caustic_scan_kernel (warp per chunk, lanes over
+// caustic segments) into d_trials, then seeds_kernel (thread per chunk, the
+// warm-start chain over the points and their trial points)
 void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const DevLens* d_lenses,
                   const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
-                  cudaStream_t st);
+                  TrialList* d_trials, cudaStream_t st);
 
 void launch_point_lc(const Traj* d_trajs, const SeedJob* d_jobs, int njobs,
                      const DevLens* d_lenses, double* d_amp, cudaStream_t st);

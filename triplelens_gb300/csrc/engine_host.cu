@@ -136,6 +136,7 @@ Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump) {
   R.points = (PointIn*)points_.need(sizeof(PointIn) * np);
   R.seeds = (int32_t*)seeds_.need(sizeof(int32_t) * 2 * kMaxSeeds * np);
   R.out = (PointOut*)out_.need(sizeof(PointOut) * np);
+  R.trials = (TrialList*)trials_.need(sizeof(TrialList) * np);
   R.dump = nullptr;
   R.dump_count = nullptr;
   R.dump_cap = 0;

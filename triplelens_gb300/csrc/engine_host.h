@@ -27,6 +27,7 @@ struct Run {
   PointIn* points;
   int32_t* seeds;
   PointOut* out;
+  TrialList* trials;
   uint32_t* dump;
   unsigned* dump_count;
   unsigned dump_cap;
@@ -64,7 +65,7 @@ class Engine {
  private:
   Engine();
   bool ensure_fill_scratch(int level);
-  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_;
+  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_, trials_;
   int want_big_ctas_ = -1;   // -1: 64 when there are >= 256 CTAs, else a quarter
   unsigned big_units_ = 0;
   void* fill_base_[kFillLevels] = {nullptr, nullptr, nullptr};

@@ -185,7 +185,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, impl->d_lens, impl->d_ca, R.points, R.seeds,
-                   R.out, E.stream);
+                   R.out, R.trials, E.stream);
   if (extSeeds) {
     // replace the seeds with the caller's, keep the positions
     std::vector<tl::PointOut> hout(np);

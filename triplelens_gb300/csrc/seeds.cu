@@ -9,11 +9,12 @@
 //                      warm-started, six roots polished on six lanes),
 //                      caustics, caustic boxes, image-plane grid.
 //                      (ccc.cc:42-203, lcirs.cc:39-92)
-//   seeds_kernel       one warp per chunk of kChainChunk consecutive points
+//   caustic_scan_kernel  one warp per chunk: caustic-segment tests of every
+//                      point (lanes over segments), trial points in order
+//   seeds_kernel       one thread per chunk of kChainChunk consecutive points
 //                      of a curve: point images through the warm-started
-//                      Laguerre chain (lane 0), caustic-segment tests on all
-//                      32 lanes (ballot gives the run starts), images of the
-//                      crossing points (lcirs.cc:117-174, imgpoint.cc:160-286)
+//                      Laguerre chain, then the images of the crossing trial
+//                      points (lcirs.cc:117-174, imgpoint.cc:160-286)
 //   point_lc_kernel    point-source magnification curve (lcbase.cc:17-52)
 #include <cuda_runtime.h>
 #include <math.h>
@@ -182,7 +183,8 @@ void launch_lens_setup(const LensSpec* d_specs, int nlens, DevLens* d_lenses, cx
 // ---------------------------------------------------------------------------
 // seeds
 // ---------------------------------------------------------------------------
-constexpr int kSeedWarps = 4;
+constexpr int kSeedThreads = 32;   // one warp per block: chains are latency-bound
+constexpr int kScanWarps = 4;
 
 __device__ __forceinline__ cx traj_pos(const Traj& T, uint32_t i) {
   double t = (double)i / (double)T.n;
@@ -214,19 +216,66 @@ __device__ __forceinline__ void emit_seeds(const Grid& g, const cx* imgs, int n,
   }
 }
 
-__global__ void __launch_bounds__(kSeedWarps * 32)
-seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* lenses,
-             const cx* ca_all, PointIn* points, int32_t* seeds_all, PointOut* out) {
+// Caustic-segment tests (lcirs.cc:131-165, 195-255): one warp per chunk, the
+// 32 lanes over consecutive segments of a branch whose box overlaps the
+// source; a warp ballot marks the first segment of every run of hits
+// (pointTaken), whose trial point is appended in segment order.
+__global__ void __launch_bounds__(kScanWarps * 32)
+caustic_scan_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* lenses,
+                    const cx* ca_all, TrialList* trials) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ji = blockIdx.x * kSeedWarps + warp;
+  const int ji = blockIdx.x * kScanWarps + warp;
+  if (ji >= njobs) return;
+  const SeedJob job = jobs[ji];
+  const Traj T = trajs[job.traj];
+  const DevLens& D = lenses[T.lens];
+  const double rho = D.rho;
+  const cx* ca = ca_all + (size_t)T.lens * kBranches * kCCLen;
+  for (int q = 0; q < job.count; q++) {
+    const uint32_t i = (uint32_t)(job.first + q);
+    const int64_t p = T.point_base + i;
+    const cx pos = traj_pos(T, i);
+    TrialList* tl = &trials[p];
+    uint32_t nt = 0;
+    if (isfinite(pos.re) && isfinite(pos.im)) {
+      for (int k = 0; k < kBranches; k++) {
+        if (!(pos.re + rho >= D.box_min[k].re && pos.re - rho <= D.box_max[k].re &&
+              pos.im + rho >= D.box_min[k].im && pos.im - rho <= D.box_max[k].im))
+          continue;
+        const cx* br = ca + k * kCCLen;
+        unsigned carry = 0;  // was the previous segment a hit
+        for (int base = 0; base < kCCLen - 1; base += 32) {
+          const int j = base + lane;
+          cx trial = mk(0.0, 0.0);
+          bool hit = false;
+          if (j < kCCLen - 1) hit = intersection_check(rho, pos, br[j], br[j + 1], &trial);
+          const unsigned m = __ballot_sync(0xffffffffu, hit);
+          const unsigned starts = m & ~((m << 1) | carry);
+          carry = (m >> 31) & 1u;
+          if ((starts >> lane) & 1u) {
+            const uint32_t slot = nt + __popc(starts & ((1u << lane) - 1u));
+            if (slot < (uint32_t)kMaxTrials) tl->t[slot] = trial;
+          }
+          nt += __popc(starts);
+        }
+      }
+    }
+    if (lane == 0) tl->n = nt;
+  }
+}
+
+// One thread per chunk: the warm-start chain is serial within a chunk, and
+// independent across chunks, so 32 chunks share a warp's FP64 instructions.
+__global__ void __launch_bounds__(kSeedThreads)
+seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* lenses,
+             PointIn* points, int32_t* seeds_all, PointOut* out, const TrialList* trials) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x;
   if (ji >= njobs) return;
   const SeedJob job = jobs[ji];
   const Traj T = trajs[job.traj];
   const DevLens& D = lenses[T.lens];
   const Lens L = D.L;
   const Grid g = D.g;
-  const double rho = D.rho;
-  const cx* ca = ca_all + (size_t)T.lens * kBranches * kCCLen;
 
   RootChain ch;
   chain_reset(&ch);
@@ -238,79 +287,55 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
     int32_t* seeds = seeds_all + (size_t)p * 2 * kMaxSeeds;
     uint32_t nseed = 0, status = 0;
     if (!(isfinite(pos.re) && isfinite(pos.im))) status |= kStBadInput;
-    if (lane == 0) {
-      PointIn pi;
-      pi.sx = pos.re;
-      pi.sy = pos.im;
-      pi.lens = T.lens;
-      pi.est_blocks = 0;
-      points[p] = pi;
-      if (!status) {
-        int n = chain_images(L, &ch, pos, imgs, &c_trig);
-        if (wrong_count(L, n)) status |= kStImageCount;
-        emit_seeds(g, imgs, n, seeds, &nseed, &status);
-        // predicted fill size, for the fill's largest-first order: the
-        // point-source magnification tracks the finite-source one closely
-        // (rays ~ A pi ppr^2), plus the boundary blocks
-        double a = 0.0;
-        for (int k = 0; k < n; k++) a += image_amp(L, imgs[k]);
-        const double est = a * 3.14159265358979 * (double)D.ppr * (double)D.ppr / 1024.0 * 1.15;
-        points[p].est_blocks = (uint32_t)fmin(fmax(est, 0.0), 4.0e9);
-      }
-    }
-    status = __shfl_sync(0xffffffffu, status, 0);
+    PointIn pi;
+    pi.sx = pos.re;
+    pi.sy = pos.im;
+    pi.lens = T.lens;
+    pi.est_blocks = 0;
     if (!(status & kStBadInput)) {
-      // caustic-crossing seeds (lcirs.cc:131-165)
-      for (int k = 0; k < kBranches; k++) {
-        if (!(pos.re + rho >= D.box_min[k].re && pos.re - rho <= D.box_max[k].re &&
-              pos.im + rho >= D.box_min[k].im && pos.im - rho <= D.box_max[k].im))
-          continue;
-        const cx* br = ca + k * kCCLen;
-        unsigned carry = 0;  // pointTaken: was the previous segment a hit
-        for (int base = 0; base < kCCLen - 1; base += 32) {
-          const int j = base + lane;
-          cx trial = mk(0.0, 0.0);
-          bool hit = false;
-          if (j < kCCLen - 1) hit = intersection_check(rho, pos, br[j], br[j + 1], &trial);
-          const unsigned m = __ballot_sync(0xffffffffu, hit);
-          unsigned starts = m & ~((m << 1) | carry);
-          carry = (m >> 31) & 1u;
-          while (starts) {
-            const int l = __ffs(starts) - 1;
-            starts &= starts - 1;
-            cx tr;
-            tr.re = __shfl_sync(0xffffffffu, trial.re, l);
-            tr.im = __shfl_sync(0xffffffffu, trial.im, l);
-            if (lane == 0) {
-              int n = chain_images(L, &ch, tr, imgs, &c_trig);
-              emit_seeds(g, imgs, n, seeds, &nseed, &status);
-            }
-          }
-        }
+      int n = chain_images(L, &ch, pos, imgs, &c_trig);
+      if (wrong_count(L, n)) status |= kStImageCount;
+      emit_seeds(g, imgs, n, seeds, &nseed, &status);
+      // predicted fill size, for the fill's largest-first order: the
+      // point-source magnification tracks the finite-source one closely
+      // (rays ~ A pi ppr^2), plus the boundary blocks
+      double a = 0.0;
+      for (int k = 0; k < n; k++) a += image_amp(L, imgs[k]);
+      const double est = a * 3.14159265358979 * (double)D.ppr * (double)D.ppr / 1024.0 * 1.15;
+      pi.est_blocks = (uint32_t)fmin(fmax(est, 0.0), 4.0e9);
+      // caustic-crossing seeds (lcirs.cc:131-165): the images of the trial
+      // points found by caustic_scan_kernel, in the reference's order
+      const TrialList& tl = trials[p];
+      const uint32_t ntr = tl.n < (uint32_t)kMaxTrials ? tl.n : (uint32_t)kMaxTrials;
+      if (tl.n > (uint32_t)kMaxTrials) status |= kStSeedOverflow;
+      for (uint32_t t = 0; t < ntr; t++) {
+        const int nt = chain_images(L, &ch, tl.t[t], imgs, &c_trig);
+        emit_seeds(g, imgs, nt, seeds, &nseed, &status);
       }
     }
-    if (lane == 0) {
-      PointOut o;
-      o.count = 0;
-      o.wsum_fx = 0;
-      o.status = status;
-      o.nseeds = nseed < (uint32_t)kMaxSeeds ? nseed : (uint32_t)kMaxSeeds;
-      o.tiles = 0;
-      o.diag = 0;
-      o.rays_eval = 0;
-      o.rays_fp64 = 0;
-      out[p] = o;
-    }
+    points[p] = pi;
+    PointOut o;
+    o.count = 0;
+    o.wsum_fx = 0;
+    o.status = status;
+    o.nseeds = nseed < (uint32_t)kMaxSeeds ? nseed : (uint32_t)kMaxSeeds;
+    o.tiles = 0;
+    o.diag = 0;
+    o.rays_eval = 0;
+    o.rays_fp64 = 0;
+    out[p] = o;
   }
 }
 
 void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const DevLens* d_lenses,
                   const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
-                  cudaStream_t st) {
+                  TrialList* d_trials, cudaStream_t st) {
   if (njobs <= 0) return;
-  int blocks = (njobs + kSeedWarps - 1) / kSeedWarps;
-  seeds_kernel<<<blocks, kSeedWarps * 32, 0, st>>>(d_jobs, njobs, d_trajs, d_lenses, d_ca, d_points,
-                                                   d_seeds, d_out);
+  caustic_scan_kernel<<<(njobs + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, st>>>(
+      d_jobs, njobs, d_trajs, d_lenses, d_ca, d_trials);
+  const int blocks = (njobs + kSeedThreads - 1) / kSeedThreads;
+  seeds_kernel<<<blocks, kSeedThreads, 0, st>>>(d_jobs, njobs, d_trajs, d_lenses, d_points, d_seeds,
+                                                d_out, d_trials);
 }
 
 // ---------------------------------------------------------------------------
