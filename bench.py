@@ -173,6 +173,64 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
+def surrogate_leg(seed, train_lenses, eval_lenses):
+    """Finite-source surrogate: train on GPU-IRS labels, then time the plain
+    IRS and the gated path on the same fresh queries (host buffers; the lens
+    set-up both share is outside the timing)."""
+    import torch
+    from triplelens_gb300 import surrogate as S
+    t_start = time.perf_counter()
+
+    def log(what):
+        print("[bench surrogate %.1fs] %s" % (time.perf_counter() - t_start, what),
+              file=sys.stderr, flush=True)
+
+    with quiet_stdout():
+        model, tinfo = S.fit(seed + 7, train_lenses, 64)
+        log("trained: %s" % tinfo)
+        q = S.QuerySet(*S.sample_config5(seed + 8, eval_lenses, 64))
+        n_drawn = q.n
+        q.restrict()
+        q.irs_points(torch.arange(min(q.n, 4096), device=q.dev))   # warm-up
+        torch.cuda.synchronize()
+        log("queries %d of %d" % (q.n, n_drawn))
+        t0 = time.perf_counter()
+        truth, st = q.label()
+        t_irs = time.perf_counter() - t0
+        log("plain IRS %.2fs" % t_irs)
+        S.evaluate(model, q)                                        # warm-up
+        mag, gated, tm = S.evaluate(model, q)
+        log("gated %s" % tm)
+    ok = (truth > 0) & ((st & 0x2f) == 0)
+    err = np.abs(mag[ok] / truth[ok] - 1.0)
+    aps = q.aps.cpu().numpy()
+    dc = q.dc.cpu().numpy()
+    # the method without the network at the same error target: A_point beyond
+    # 5 source radii of the caustic, IRS within
+    ps_gate = dc < 5.0
+    err_ps = np.abs(np.where(ps_gate, truth, aps)[ok] / truth[ok] - 1.0)
+    return {
+        "queries": int(q.n), "queries_drawn": int(n_drawn),
+        "train_points": tinfo["train_points"],
+        "label_s": round(tinfo["label_s"], 2), "train_s": round(tinfo["train_s"], 2),
+        "train_steps": tinfo["steps"],
+        "plain_irs_points_per_s": q.n / t_irs,
+        "gated_points_per_s": q.n / tm["total_s"],
+        "speedup_vs_plain_irs": t_irs / tm["total_s"],
+        "fallback_fraction": len(gated) / q.n,
+        "median_rel_err": float(np.median(err)), "p99_rel_err": float(np.percentile(err, 99)),
+        "gated_time_s": {k: round(v, 4) for k, v in tm.items()},
+        "gate": S.GATE,
+        "point_source_only": {"fallback_fraction": float(ps_gate.mean()),
+                              "median_rel_err": float(np.median(err_ps)),
+                              "p99_rel_err": float(np.percentile(err_ps, 99))},
+        "workload": "lenses as config 2, rho log-uniform [1e-4, 3e-2], v uniform [0.3, 0.7], "
+                    "500 rays/radius; queries: caustic sample + offset uniform in a 3 theta_E "
+                    "disc; training sources 2-300 rho from a caustic; queries with A_point > "
+                    "300 (sources within ~rho of a cusp at small rho) left out of both arms",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -184,6 +242,11 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-sample", type=int, default=512, help="points timed on the CPU")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--sur-train-lenses", type=int, default=1024,
+                    help="surrogate training lenses (64 sources each)")
+    ap.add_argument("--sur-eval-lenses", type=int, default=16384,
+                    help="surrogate evaluation lenses (64 queries each)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -363,6 +426,8 @@ def main():
         "clocks": clocks,
         "gpu_launches": 6 * args.steps,
     }
+    if rank == 0 and not args.no_surrogate:
+        line["surrogate"] = surrogate_leg(args.seed, args.sur_train_lenses, args.sur_eval_lenses)
     if pool is not None and rank == 0:
         pts_s, pts_s1, rays_s, desc, busy = cpu_baseline(pool, ncpu, lenses, trajs, n,
                                                          args.cpu_sample)

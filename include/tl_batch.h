@@ -13,7 +13,8 @@
  * Lens parameter rows (8 doubles): a, b, th, m2, m3, rho, ld_v, ppr, where
  * ld_v >= 0 selects the v-normalised linear limb darkening ("linear", v)
  * and ld_v < 0 the reference's default model (A = 0.6, B = 0.4).
- * Trajectory rows (4 doubles): x0, y0, x1, y1.
+ * Trajectory rows (4 doubles): x0, y0, x1, y1.  A trajectory of length
+ * n = 0 is one source position (x0, y0) (one point, its own chain).
  *
  * Return values: >= 0 success (number of points for runs), < 0 error
  * (-1 bad argument, -2 CUDA error).

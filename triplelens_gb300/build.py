@@ -31,12 +31,13 @@ UNITS = [
     ("lcirs_abi.cu", []),
     ("batch_abi.cu", []),
     ("noalloc_abi.cu", []),
+    ("surrogate.cu", []),
     ("ccc_abi.cu", ["--fmad=false"]),
 ]
 
 LIBS = {
     "liblcirs.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
-                    "noalloc_abi.cu"],
+                    "noalloc_abi.cu", "surrogate.cu"],
     "libccc.so": ["seeds.cu", "engine_host.cu", "fill.cu", "ccc_abi.cu"],
 }
 

@@ -7,24 +7,12 @@
 #include <mutex>
 #include <vector>
 
+#include "batch_internal.h"
 #include "engine.h"
 #include "engine_host.h"
 #include "tl_batch.h"
 
 using tl::cx;
-
-struct tl_batch {
-  int nlens = 0;
-  tl::DevBuf specs, lenses, cc, ca;
-  std::vector<tl::DevLens> hlens;
-  int ntraj = 0;
-  long npoints = 0;
-  int njobs = 0;
-  tl::DevBuf trajs, jobs, points, seeds, out, amp, trials;
-  std::vector<tl::Traj> htraj;
-  int precision = 1;
-  uint64_t stats[4] = {0, 0, 0, 0};
-};
 
 namespace {
 
@@ -97,7 +85,7 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
   std::vector<tl::SeedJob> jobs;
   long base = 0;
   for (int i = 0; i < ntraj; i++) {
-    if (lens_idx[i] < 0 || lens_idx[i] >= b->nlens || n[i] == 0) return -1;
+    if (lens_idx[i] < 0 || lens_idx[i] >= b->nlens) return -1;
     tl::Traj& T = b->htraj[i];
     T.x0 = t4[4 * (size_t)i];
     T.y0 = t4[4 * (size_t)i + 1];

@@ -1,0 +1,22 @@
+// batch_internal.h - the batch object behind include/tl_batch.h, shared by
+// batch_abi.cu and surrogate.cu.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "engine.h"
+#include "engine_host.h"
+
+struct tl_batch {
+  int nlens = 0;
+  tl::DevBuf specs, lenses, cc, ca;
+  std::vector<tl::DevLens> hlens;
+  int ntraj = 0;
+  long npoints = 0;
+  int njobs = 0;
+  tl::DevBuf trajs, jobs, points, seeds, out, amp, trials;
+  std::vector<tl::Traj> htraj;
+  int precision = 1;
+  uint64_t stats[4] = {0, 0, 0, 0};
+};

@@ -186,8 +186,10 @@ void launch_lens_setup(const LensSpec* d_specs, int nlens, DevLens* d_lenses, cx
 constexpr int kSeedThreads = 32;   // one warp per block: chains are latency-bound
 constexpr int kScanWarps = 4;
 
+// point i of a curve (t = i/n); a curve of length n = 0 is the single
+// position (x0, y0)
 __device__ __forceinline__ cx traj_pos(const Traj& T, uint32_t i) {
-  double t = (double)i / (double)T.n;
+  double t = T.n ? (double)i / (double)T.n : 0.0;
   cx s = mk(T.x0, T.y0), e = mk(T.x1, T.y1);
   return add(s, scale(sub(e, s), t));
 }
