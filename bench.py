@@ -424,7 +424,9 @@ def main():
                  "accepted_per_s": float(stats[3]) * world / (ms_step / 1e3),
                  "status_or": int(np.bitwise_or.reduce(st))},
         "clocks": clocks,
-        "gpu_launches": 6 * args.steps,
+        # per step: caustic scan + seeds, 3 ordering kernels, the fill, and two
+        # overflow levels (collect + fill each)
+        "gpu_launches": 10 * args.steps,
     }
     if rank == 0 and not args.no_surrogate:
         line["surrogate"] = surrogate_leg(args.seed, args.sur_train_lenses, args.sur_eval_lenses)
