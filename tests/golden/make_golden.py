@@ -79,6 +79,67 @@ def read_amoeba(path):
     return t[np.lexsort((t[:, 1], t[:, 0]))]
 
 
+# critical-curve / caustic cases for libccc.so: (a, b, th, m2, m3, length);
+# m3 == 0 takes the reference's binary path
+CCC_CASES = [
+    (1.0, 0.9433981132056603, 1.0121970114513341, 0.2, 0.1, 500),
+    (1.0, 0.9433981132056603, 1.0121970114513341, 0.2, 0.1, 333),
+    (0.7, 1.4, 2.3, 0.05, 0.002, 500),
+    (1.2, 0.0, 0.0, 0.3, 0.0, 500),
+    (0.8, 1.0, 0.5, 0.1, 0.0, 400),
+]
+
+
+def ccc_worker(spec):
+    """Child process: one reference CCC object (its stdout is C++ cout)."""
+    L = ctypes.cdll.LoadLibrary(spec["lib"])
+    d, vp = ctypes.c_double, ctypes.c_void_p
+    L.ccc_new.argtypes = [d] * 5 + [ctypes.c_int]
+    L.ccc_new.restype = vp
+    L.get_cc.argtypes = [vp]
+    L.get_ca.argtypes = [vp]
+    L.print_ccc.argtypes = [vp, ctypes.c_char_p]
+    L.copy_cc_ca.argtypes = [vp, vp, vp]
+    L.copy_lenses.argtypes = [vp, vp]
+    L.get_bounding_box.argtypes = [vp, vp, vp, vp, vp, d]
+    a, b, th, m2, m3, length = spec["case"]
+    o = L.ccc_new(a, b, th, m2, m3, length)
+    # the reference's scripts call get_ca alone (run_amoebae*.py); a binary
+    # lens must take that route (get_cc first leaves it with more critical-
+    # curve than caustic branches, which copy_cc_ca then reads past)
+    if m3 != 0.0:
+        L.get_cc(o)
+    L.get_ca(o)
+    order = 4 if m3 == 0.0 else 6
+    cc = np.zeros(order * length, np.complex128)
+    ca = np.zeros(order * length, np.complex128)
+    L.copy_cc_ca(o, cc.ctypes.data_as(vp), ca.ctypes.data_as(vp))
+    lz = np.zeros(3, np.complex128)
+    L.copy_lenses(o, lz.ctypes.data_as(vp))
+    box = np.zeros(4, np.complex128)
+    L.get_bounding_box(o, *[box[k:].ctypes.data_as(vp) for k in range(4)], 1.1)
+    L.print_ccc(o, spec["file"].encode())
+    np.savez(spec["out"], cc=cc, ca=ca, lenses=lz, box=box)
+
+
+def ccc_fixtures(lib):
+    out = {"cases": np.array(CCC_CASES)}
+    with tempfile.TemporaryDirectory() as td:
+        for k, case in enumerate(CCC_CASES):
+            spec = {"lib": lib, "case": case, "file": os.path.join(td, "ccc_%d.txt" % k),
+                    "out": os.path.join(td, "ccc_%d.npz" % k)}
+            r = subprocess.run([sys.executable, __file__, "--ccc-worker", json.dumps(spec)],
+                               capture_output=True, text=True, check=True)
+            z = np.load(spec["out"])
+            for key in ("cc", "ca", "lenses", "box"):
+                out["%s_%d" % (key, k)] = z[key]
+            if k in (0, 3):   # one triple and one binary print_ccc file
+                with open(spec["file"]) as f:
+                    out["text_%d" % k] = np.array(f.read())
+            out["stdout_%d" % k] = np.array(r.stdout)
+    return out
+
+
 def ccc_and_images(lib, lens, positions):
     L = ctypes.cdll.LoadLibrary(lib)
     d = ctypes.c_double
@@ -113,12 +174,22 @@ def main():
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--worker")
     ap.add_argument("--c2", action="store_true", help="also the 5000-point config-2 curve")
+    ap.add_argument("--ccc-worker")
+    ap.add_argument("--only-ccc", action="store_true")
     args = ap.parse_args()
     if args.worker:
         worker(json.loads(args.worker))
         return
+    if args.ccc_worker:
+        ccc_worker(json.loads(args.ccc_worker))
+        return
     subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", "REF=" + args.ref], cwd=ROOT,
                    check=True)
+
+    np.savez_compressed(os.path.join(HERE, "ccc.npz"), **ccc_fixtures(REF_LIBS["fast"]))
+    print("wrote ccc.npz")
+    if args.only_ccc:
+        return
 
     lens, traj, n = workloads.config1()
     out = {"lens": lens, "traj": traj, "n": n}

@@ -238,3 +238,50 @@ def test_bad_input_reports_status(product_lib):
     st = lc.status()
     assert st[0] & 32 and lc.last_status() & 32
     assert lc.counts()[0] == 0
+
+
+def _caustics(a, b, th, m2, m3):
+    import os as _os
+    from triplelens_gb300.ccc import CCC
+    from triplelens_gb300.lcirs import LIB_DIR
+    c = CCC(a, b, th, m2, m3, 500, lib_path=_os.path.join(LIB_DIR, "libccc.so"))
+    c.get_ca()
+    cc = np.zeros(3000, np.cdouble)
+    ca = np.zeros(3000, np.cdouble)
+    c.copy_cc_ca(cc, ca)
+    return ca.reshape(6, 500)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_config3_caustic_crossing(product_lib, oracle_lib, precision):
+    """Config 3: config-2 lenses resampled until the trajectory crosses a
+    caustic; 101 points over a window of +-20 source radii around the first
+    crossing.  Seeds and ray counts equal the oracle's (FP64 IRS); the
+    split-precision map re-evaluates only a small fraction of the rays in
+    FP64; magnification error per point within the LD tolerance."""
+    lenses, trajs, _ = workloads.config3(5, _caustics, n_curves=2)
+    n = 100
+    for k in range(len(lenses)):
+        L, t = lenses[k], trajs[k]
+        tc = workloads.crossings(t, _caustics(*L[:5]))[0]
+        p0, d = t[:2], t[2:] - t[:2]
+        w = 20.0 * L[5] / np.hypot(*d)
+        win = np.concatenate([p0 + (tc - w) * d, p0 + (tc + w) * d])
+        lc = _lc(product_lib, L, n, precision)
+        lc.get_lc_irs(*win)
+        assert lc.last_status() & 0x2d == 0
+        o = _oracle(oracle_lib, L, n)
+        oseeds, ocnt, fragile = o.lc_seeds(*win)
+        gseeds, gcnt = lc.seeds()
+        assert _seed_sets(gseeds, gcnt) == _seed_sets(oseeds, ocnt), k
+        oamps, ocounts = o.lc_irs(*win)
+        counts = lc.counts()
+        assert np.array_equal(counts, ocounts), (k, np.nonzero(counts != ocounts)[0])
+        err = np.abs(lc.lc_full() - oamps) / oamps
+        assert np.max(err) < (LD_RTOL_FP64 if precision == 0 else LD_RTOL_SPLIT)
+        ev, ev64, _ = lc.stats()
+        frac64 = float(ev64) / float(ev)
+        print("config3 curve %d precision %d: FP64 fraction %.3e, max rel err %.2e, "
+              "counts %d..%d" % (k, precision, frac64, err.max(), counts.min(), counts.max()))
+        if precision == 1:
+            assert frac64 < 1e-2

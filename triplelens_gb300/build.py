@@ -38,7 +38,7 @@ UNITS = [
 LIBS = {
     "liblcirs.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
                     "noalloc_abi.cu", "surrogate.cu"],
-    "libccc.so": ["seeds.cu", "engine_host.cu", "fill.cu", "ccc_abi.cu"],
+    "libccc.so": ["ccc_abi.cu"],
 }
 
 

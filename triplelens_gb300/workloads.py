@@ -11,7 +11,8 @@ config2  random triple lenses: mass ratios log-uniform in [1e-3, 1] (masses
          [0.5, 2], angle uniform; trajectory angle uniform, impact parameter
          uniform in [-0.5, 0.5], 4 theta_E, 5000 points; rho = 1e-3,
          500 rays per radius, linear limb darkening v = 0.5.
-config3  config2 lenses resampled until the trajectory crosses a caustic.
+config3  config2 lenses resampled until the trajectory crosses a caustic
+         (the caustics come from libccc.so).
 config4  many curves, each its own config2 lens, rho log-uniform in
          [1e-4, 3e-2], rays per radius in {200, 500, 1000}, v in [0.3, 0.7].
 
@@ -62,6 +63,40 @@ def config2(seed, n_curves=1, n_points=5000, rho=1e-3, ppr=500, ld_v=0.5):
         a, b, th, m2, m3 = _random_lens(rng)
         lenses.append([a, b, th, m2, m3, rho, ld_v, float(ppr)])
         trajs.append(_random_traj(rng))
+    return np.array(lenses), np.array(trajs), n_points
+
+
+def crossings(traj, ca):
+    """Parameters t in [0, 1] (sorted) at which the trajectory x0,y0 -> x1,y1
+    crosses the caustic polylines ca (branches, samples; complex, closed)."""
+    ca = np.asarray(ca)
+    p0, p1 = np.asarray(traj[:2]), np.asarray(traj[2:])
+    q = np.stack([ca.real, ca.imag], axis=-1)
+    q0 = q.reshape(-1, 2)
+    q1 = np.roll(q, -1, axis=1).reshape(-1, 2)
+    d = p1 - p0
+    e = q1 - q0
+    den = d[0] * e[:, 1] - d[1] * e[:, 0]
+    w = q0 - p0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t = (w[:, 0] * e[:, 1] - w[:, 1] * e[:, 0]) / den
+        u = (w[:, 0] * d[1] - w[:, 1] * d[0]) / den
+    hit = (den != 0) & (t >= 0) & (t <= 1) & (u >= 0) & (u <= 1)
+    return np.sort(t[hit])
+
+
+def config3(seed, caustics, n_curves=1, n_points=5000, rho=1e-3, ppr=500, ld_v=0.5):
+    """config2 lenses and trajectories, resampled until the trajectory crosses
+    a caustic branch.  caustics(a, b, th, m2, m3) returns the caustic samples
+    as an array (branches, samples) of complex numbers (e.g. from libccc.so)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lenses, trajs = [], []
+    while len(lenses) < n_curves:
+        a, b, th, m2, m3 = _random_lens(rng)
+        traj = _random_traj(rng)
+        if len(crossings(traj, caustics(a, b, th, m2, m3))):
+            lenses.append([a, b, th, m2, m3, rho, ld_v, float(ppr)])
+            trajs.append(traj)
     return np.array(lenses), np.array(trajs), n_points
 
 
