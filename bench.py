@@ -173,6 +173,52 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
+def config4_leg(seed, curves, reps):
+    """Config 4 (sub-sample): `curves` light curves of 2000 points, each its
+    own random lens with rho log-uniform in [1e-4, 3e-2], 200/500/1000 rays
+    per radius and v in [0.3, 0.7]; launch shape from the autotuner; seeds +
+    fill replayed as one CUDA graph (device-resident inputs)."""
+    import torch
+    from triplelens_gb300 import workloads
+    from triplelens_gb300.batch import Batch
+    lenses, trajs, n = workloads.config4(seed + 3, n_curves=curves)
+    b = Batch()
+    b.set_lenses(lenses)
+    npts = b.set_trajectories(trajs, np.arange(curves), np.full(curves, n))
+    t0 = time.perf_counter()
+    chosen, times = b.autotune(sample_points=min(npts, 32768))
+    t_tune = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    b.graph_capture()
+    b.graph_launch(stream.cuda_stream)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.graph_launch(stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    ms_graph = e0.elapsed_time(e1) / reps
+    e0.record(stream)
+    b.run_device(3, stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    ms_plain = e0.elapsed_time(e1)
+    _, cnt, st = b.download(stream.cuda_stream)
+    stats = b.stats()
+    return {"workload": "config 4 sub-sample: %d curves x %d points, own lens each" % (curves, n + 1),
+            "points": int(npts), "ms_per_replay": ms_graph, "points_per_s": npts / (ms_graph / 1e3),
+            "rays_evaluated_per_s": float(stats[0]) / (ms_graph / 1e3),
+            "ms_plain_launches": ms_plain,
+            "autotune": {"block_h": chosen[0], "ctas_per_sm": chosen[1], "points_timed": chosen[2],
+                         "candidates_ms": {"32x2": float(times[0]), "32x3": float(times[1]),
+                                           "32x4": float(times[2]), "16x2": float(times[3]),
+                                           "8x2": float(times[4])},
+                         "seconds": round(t_tune, 2)},
+            "status_or": int(np.bitwise_or.reduce(st))}
+
+
 def surrogate_leg(seed, train_lenses, eval_lenses):
     """Finite-source surrogate: train on GPU-IRS labels, then time the plain
     IRS and the gated path on the same fresh queries (host buffers; the lens
@@ -219,6 +265,10 @@ def surrogate_leg(seed, train_lenses, eval_lenses):
         "speedup_vs_plain_irs": t_irs / tm["total_s"],
         "fallback_fraction": len(gated) / q.n,
         "median_rel_err": float(np.median(err)), "p99_rel_err": float(np.percentile(err, 99)),
+        "plain_irs_status_counts": {"table_full": int(((st & 4) != 0).sum()),
+                                    "timeout": int(((st & 8) != 0).sum()),
+                                    "edge": int(((st & 2) != 0).sum()),
+                                    "image_count": int(((st & 16) != 0).sum())},
         "gated_time_s": {k: round(v, 4) for k, v in tm.items()},
         "gate": S.GATE,
         "point_source_only": {"fallback_fraction": float(ps_gate.mean()),
@@ -243,6 +293,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512, help="points timed on the CPU")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-config4", action="store_true")
+    ap.add_argument("--c4-curves", type=int, default=64,
+                    help="config-4 sub-sample: curves of 2000 points, each its own lens")
     ap.add_argument("--sur-train-lenses", type=int, default=1024,
                     help="surrogate training lenses (64 sources each)")
     ap.add_argument("--sur-eval-lenses", type=int, default=16384,
@@ -428,6 +481,8 @@ def main():
         # overflow levels (collect + fill each)
         "gpu_launches": 10 * args.steps,
     }
+    if rank == 0 and not args.no_config4:
+        line["config4"] = config4_leg(args.seed, args.c4_curves, max(1, min(args.steps, 3)))
     if rank == 0 and not args.no_surrogate:
         line["surrogate"] = surrogate_leg(args.seed, args.sur_train_lenses, args.sur_eval_lenses)
     if pool is not None and rank == 0:

@@ -70,6 +70,25 @@ int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int
  * current trajectories, n points each, written to amp (host). */
 long tlb_point_lc(tl_batch* b, double* amp);
 
+/* Autotuner: runs the seeds of the current trajectories, then times the
+ * fill over their first sample_points points (all if <= 0) for the launch
+ * shapes (block height = rows of the 32-column frontier blocks, resident
+ * fill CTAs per SM) (32, 2), (32, 3), (32, 4), (16, 2), (8, 2), and keeps
+ * the fastest for later runs of the process.  chosen3 = {block height, CTAs
+ * per SM, points timed}; times_ms (5 floats, may be NULL) the fill times in
+ * that order.  Results do not depend on the choice (the filled sets are
+ * exact). */
+int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times_ms);
+
+/* Captures seeds + fill of the current trajectories (one warm run first,
+ * so the captured run allocates nothing) into a CUDA graph on the engine's
+ * stream.  tlb_graph_launch replays it on `stream` (NULL: the engine's);
+ * the trajectories may be replaced through tlb_set_trajectories between
+ * replays if their counts stay the same.  Results are read with
+ * tlb_download as after tlb_run_device. */
+int tlb_graph_capture(tl_batch* b);
+int tlb_graph_launch(tl_batch* b, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -285,3 +285,39 @@ def test_config3_caustic_crossing(product_lib, oracle_lib, precision):
               "counts %d..%d" % (k, precision, frac64, err.max(), counts.min(), counts.max()))
         if precision == 1:
             assert frac64 < 1e-2
+
+
+def test_config4_graph_and_autotune(product_lib):
+    """Config 4 (sub-sample: 8 curves x 301 points, each its own lens, rho
+    log-uniform in [1e-4, 3e-2], 200/500/1000 rays per radius): the counts
+    do not depend on the autotuner's launch shape, and a CUDA-graph replay
+    gives the plain run's counts, also after the trajectories are replaced."""
+    from triplelens_gb300.batch import Batch
+    lenses, trajs, _ = workloads.config4(3, n_curves=8)
+    n = 300
+    b = Batch(lib_path=product_lib)
+    b.set_lenses(lenses)
+    idx = np.arange(len(trajs))
+    b.set_trajectories(trajs, idx, np.full(len(trajs), n))
+    b.run_device(3)
+    amp0, cnt0, st0 = b.download()
+    assert np.bitwise_or.reduce(st0) & 0x2d == 0
+    chosen, times = b.autotune(sample_points=1000)
+    assert chosen[0] in (8, 16, 32) and chosen[1] in (2, 3, 4)
+    assert np.all(times[times >= 0] > 0)
+    b.run_device(3)
+    amp1, cnt1, _ = b.download()
+    assert np.array_equal(cnt1, cnt0)
+    assert np.max(np.abs(amp1 - amp0) / amp0) < LD_RTOL_SPLIT
+    b.graph_capture()
+    b.graph_launch()
+    amp2, cnt2, _ = b.download()
+    assert np.array_equal(cnt2, cnt0)
+    # new trajectories, same counts: replay equals a plain run
+    _, trajs2, _ = workloads.config4(4, n_curves=8)
+    b.set_trajectories(trajs2, idx, np.full(len(trajs2), n))
+    b.graph_launch()
+    _, cnt3, _ = b.download()
+    b.run_device(3)
+    _, cnt4, _ = b.download()
+    assert np.array_equal(cnt3, cnt4)

@@ -39,6 +39,13 @@ def _bind(L):
     L.tlb_configure.restype = ctypes.c_int
     L.tlb_point_lc.argtypes = [vp, f64]
     L.tlb_point_lc.restype = ctypes.c_long
+    L.tlb_autotune.argtypes = [vp, ctypes.c_long, ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"),
+                               ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")]
+    L.tlb_autotune.restype = ctypes.c_int
+    L.tlb_graph_capture.argtypes = [vp]
+    L.tlb_graph_capture.restype = ctypes.c_int
+    L.tlb_graph_launch.argtypes = [vp, vp]
+    L.tlb_graph_launch.restype = ctypes.c_int
     _bound.add(id(L))
     return L
 
@@ -115,6 +122,26 @@ class Batch:
         out = np.zeros(4, np.uint64)
         self.L.tlb_stats(self.obj, out)
         return out
+
+    def autotune(self, sample_points=0):
+        """Fastest fill launch shape on a prefix of the current points:
+        (block height, CTAs per SM, points timed), and the 5 timings (ms)."""
+        chosen = np.zeros(3, np.int32)
+        times = np.zeros(5, np.float32)
+        r = self.L.tlb_autotune(self.obj, sample_points, chosen, times)
+        if r < 0:
+            raise RuntimeError("tlb_autotune failed: %d" % r)
+        return tuple(int(x) for x in chosen), times
+
+    def graph_capture(self):
+        r = self.L.tlb_graph_capture(self.obj)
+        if r < 0:
+            raise RuntimeError("tlb_graph_capture failed: %d" % r)
+
+    def graph_launch(self, stream=None):
+        r = self.L.tlb_graph_launch(self.obj, stream)
+        if r < 0:
+            raise RuntimeError("tlb_graph_launch failed: %d" % r)
 
     def point_lc(self):
         amp = np.zeros(self.npoints)

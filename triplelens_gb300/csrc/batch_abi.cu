@@ -31,6 +31,7 @@ tl_batch* tlb_new(void) {
 
 void tlb_delete(tl_batch* b) {
   if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
   for (tl::DevBuf* d : {&b->specs, &b->lenses, &b->cc, &b->ca, &b->trajs, &b->jobs, &b->points,
                         &b->seeds, &b->out, &b->amp, &b->trials})
     if (d->p) cudaFree(d->p);
@@ -202,6 +203,105 @@ int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int
   std::lock_guard<std::mutex> g(E.mu);
   E.set_fill_config(fill_ctas, table_log2, threads, block_h);
   return 0;
+}
+
+int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times_ms) {
+  if (!b || b->npoints <= 0 || !chosen3) return -1;
+  tl::Engine& E = tl::Engine::get();
+  const long np = sample_points > 0 && sample_points < b->npoints ? sample_points : b->npoints;
+  // seeds of every point once; candidates time the fill of the first np
+  if (tlb_run_device(b, 1, nullptr) < 0) return -2;
+  // the 8- and 16-row kernels are compiled for 2 CTAs per SM only
+  const int cand[5][2] = {{32, 2}, {32, 3}, {32, 4}, {16, 2}, {8, 2}};
+  float best = 3.0e38f;
+  int best_bh = E.block_h(), best_occ = tl::fill_occupancy();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int k = 0;
+  for (const auto& c : cand) {
+    {
+      const int bh = c[0], occ = c[1];
+      float ms = -1.f;
+      {
+        std::lock_guard<std::mutex> g(E.mu);
+        E.set_fill_config(0, 0, 0, bh, occ);
+        tl::Run R;
+        R.trajs = (tl::Traj*)b->trajs.p;
+        R.jobs = (tl::SeedJob*)b->jobs.p;
+        R.points = (tl::PointIn*)b->points.p;
+        R.seeds = (int32_t*)b->seeds.p;
+        R.out = (tl::PointOut*)b->out.p;
+        R.trials = (tl::TrialList*)b->trials.p;
+        R.dump = nullptr;
+        R.dump_count = nullptr;
+        R.dump_cap = 0;
+        for (int rep = 0; rep < 2; rep++) {   // the first run allocates the tables
+          cudaEventRecord(e0, E.stream);
+          E.fill_on(R, (size_t)np, (const tl::DevLens*)b->lenses.p, b->precision, E.stream);
+          cudaEventRecord(e1, E.stream);
+          if (!E.check(cudaEventSynchronize(e1))) break;
+          cudaEventElapsedTime(&ms, e0, e1);
+        }
+      }
+      if (times_ms) times_ms[k] = ms;
+      k++;
+      if (ms > 0.f && ms < best) {
+        best = ms;
+        best_bh = bh;
+        best_occ = occ;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  {
+    std::lock_guard<std::mutex> g(E.mu);
+    E.set_fill_config(0, 0, 0, best_bh, best_occ);
+  }
+  chosen3[0] = best_bh;
+  chosen3[1] = best_occ;
+  chosen3[2] = (int32_t)np;
+  return 0;
+}
+
+int tlb_graph_capture(tl_batch* b) {
+  if (!b || b->npoints <= 0) return -1;
+  tl::Engine& E = tl::Engine::get();
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  // a warm run allocates every buffer and table level the run touches, so
+  // the captured run allocates nothing
+  if (tlb_run_device(b, 3, nullptr) < 0) return -2;
+  if (!E.check(cudaStreamSynchronize(E.stream))) return -2;
+  cudaGraph_t graph = nullptr;
+  if (!E.check(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal))) return -2;
+  const int r = tlb_run_device(b, 3, nullptr);
+  const cudaError_t ce = cudaStreamEndCapture(E.stream, &graph);
+  if (r < 0 || ce != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return -2;
+  }
+  const cudaError_t ie = cudaGraphInstantiate(&b->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    b->graph = nullptr;
+    cudaGetLastError();
+    return -2;
+  }
+  b->graph_points = b->npoints;
+  b->graph_jobs = b->njobs;
+  return 0;
+}
+
+int tlb_graph_launch(tl_batch* b, void* stream) {
+  if (!b || !b->graph) return -1;
+  if (b->npoints != b->graph_points || b->njobs != b->graph_jobs) return -1;
+  tl::Engine& E = tl::Engine::get();
+  return E.check(cudaGraphLaunch(b->graph, pick(stream))) ? 0 : -2;
 }
 
 long tlb_point_lc(tl_batch* b, double* amp) {

@@ -19,4 +19,8 @@ struct tl_batch {
   std::vector<tl::Traj> htraj;
   int precision = 1;
   uint64_t stats[4] = {0, 0, 0, 0};
+  // captured seeds + fill of the current trajectories (tlb_graph_capture)
+  cudaGraphExec_t graph = nullptr;
+  long graph_points = 0;
+  int graph_jobs = 0;
 };

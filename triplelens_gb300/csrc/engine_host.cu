@@ -79,15 +79,17 @@ bool Engine::check(cudaError_t e) {
   return true;
 }
 
-void Engine::set_fill_config(int ctas, int cap_log2, int threads, int block_h) {
+void Engine::set_fill_config(int ctas, int cap_log2, int threads, int block_h, int occ) {
   if (ctas > 0) want_ctas_ = ctas;
   if (cap_log2 > 0) want_cap_log2_ = cap_log2;
   if (threads > 0) threads_ = threads;
+  if (occ >= 2 && occ <= 4) set_fill_occupancy(occ);
   const bool bh_changed = (block_h == 8 || block_h == 16 || block_h == 32) && block_h != block_h_;
   if (bh_changed) block_h_ = block_h;
+  const int ctas0 = want_ctas_ > 0 ? want_ctas_ : fill_default_ctas();
   for (int level = 0; level < kFillLevels; level++) {
     if (!fs_[level].keys) continue;
-    if (bh_changed || (level == 0 && (fs_[0].ctas != want_ctas_ ||
+    if (bh_changed || (level == 0 && (fs_[0].ctas != ctas0 ||
                                       fs_[0].cap_log2 + (block_h_ == 32 ? 2 : (block_h_ == 16 ? 1 : 0)) !=
                                           want_cap_log2_))) {
       cudaStreamSynchronize(stream);

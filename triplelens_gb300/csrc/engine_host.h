@@ -58,8 +58,8 @@ class Engine {
   int fill_ctas() const { return fs_[0].ctas; }
   int fill_cap_log2() const { return fs_[0].cap_log2; }
   // fill launch shape; values <= 0 keep the current setting; block_h is the
-  // rows per block (8, 16 or 32)
-  void set_fill_config(int ctas, int cap_log2, int threads, int block_h = 0);
+  // rows per block (8, 16 or 32), occ the resident CTAs per SM (2, 3 or 4)
+  void set_fill_config(int ctas, int cap_log2, int threads, int block_h = 0, int occ = 0);
   int block_h() const { return block_h_; }
 
  private:
@@ -68,7 +68,7 @@ class Engine {
   DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_, trials_;
   int want_big_ctas_ = -1;   // -1: 64 when there are >= 256 CTAs, else a quarter
   unsigned big_units_ = 0;
-  void* fill_base_[kFillLevels] = {nullptr, nullptr, nullptr};
+  void* fill_base_[kFillLevels] = {};
   FillScratch fs_[kFillLevels]{};
   int want_ctas_ = 0, want_cap_log2_ = 17, threads_ = 256;
   int levels_ = kFillLevels;
