@@ -281,6 +281,22 @@ def surrogate_leg(seed, train_lenses, eval_lenses):
     }
 
 
+def rank_seed(seed, rank):
+    """Weak scaling: every rank draws its own curves (independent objects,
+    no data-path collective)."""
+    return seed + 1000 * rank
+
+
+def max_over_ranks(value, dist, device):
+    """The slowest rank's step time (the only collective of the bench)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,7 +324,7 @@ def main():
 
     from triplelens_gb300 import workloads
     # weak scaling: every rank its own curves
-    lenses, trajs, n = workloads.config2(args.seed + 1000 * rank, n_curves=args.curves,
+    lenses, trajs, n = workloads.config2(rank_seed(args.seed, rank), n_curves=args.curves,
                                         n_points=args.points)
     config = {"workload": "config2: %d random triple lenses x %d-point curves, rho=1e-3, "
                           "500 rays/radius, linear LD v=0.5" % (args.curves, n),
@@ -408,9 +424,7 @@ def main():
         time.sleep(0.3)
     torch.cuda.synchronize()
     if dist:
-        t = torch.tensor([tot_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
+        tot_ms = max_over_ranks(tot_ms, dist, "cuda")
         dist.barrier()
     ms_step = tot_ms / args.steps
     value = npts * world / (ms_step / 1e3)
