@@ -204,6 +204,52 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint
 
 constexpr int kBM = 64, kBN = 64, kBK = 32, kPitch = kBK + 8;
 
+// Stages the 64 x 32 tile T(r, c) = P[(r0 + r) * s_r + (c0 + c) * s_c] (zero
+// outside r < rmax, c < cmax) into S[r][c] with 128 threads.  16-byte loads
+// along whichever direction is contiguous when the rows (or columns) are
+// 16-byte aligned and the tile is whole in that direction; element loads
+// otherwise.
+__device__ __forceinline__ void stage_tile(uint16_t (*S)[kPitch], const uint16_t* P, long s_r,
+                                           long s_c, int r0, int rmax, int c0, int cmax,
+                                           int tid) {
+  const bool aligned = ((uintptr_t)P & 15) == 0;
+  if (aligned && s_c == 1 && (s_r & 7) == 0 && c0 + kBK <= cmax) {
+    // 4 vectors per row along c
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const int e = tid + i * 128;
+      const int r = e >> 2, q = e & 3;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r0 + r < rmax) v = *reinterpret_cast<const uint4*>(P + (long)(r0 + r) * s_r + c0 + q * 8);
+      *reinterpret_cast<uint4*>(&S[r][q * 8]) = v;
+    }
+    return;
+  }
+  if (aligned && s_r == 1 && (s_c & 7) == 0 && r0 + kBM <= rmax) {
+    // 8 vectors per column along r, scattered into the rows
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const int e = tid + i * 128;
+      const int c = e >> 3, q = e & 7;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (c0 + c < cmax) v = *reinterpret_cast<const uint4*>(P + (long)(c0 + c) * s_c + r0 + q * 8);
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        S[q * 8 + 2 * j][c] = (uint16_t)(w[j] & 0xffffu);
+        S[q * 8 + 2 * j + 1][c] = (uint16_t)(w[j] >> 16);
+      }
+    }
+    return;
+  }
+  for (int e = tid; e < kBM * kBK; e += 128) {
+    int r, c;
+    if (s_c == 1) { r = e / kBK; c = e % kBK; } else { c = e / kBM; r = e % kBM; }
+    const int m = r0 + r, k = c0 + c;
+    S[r][c] = (m < rmax && k < cmax) ? P[(long)m * s_r + (long)k * s_c] : (uint16_t)0;
+  }
+}
+
 // C[m][n] = sum_k A(m,k) B(k,n), A(m,k) = A[m*a_sm + k*a_sk], B(k,n) =
 // B[k*b_sk + n*b_sn]; blockIdx.z splits k into chunks of k_split.
 template <int EPI>
@@ -231,19 +277,8 @@ gemm_bf16_kernel(int M, int N, int K, const __nv_bfloat16* A, long a_sm, long a_
       for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
 
   for (int k0 = kbeg; k0 < kend; k0 += kBK) {
-    // consecutive threads walk the operand's contiguous direction
-    for (int e = tid; e < kBM * kBK; e += 128) {
-      int r, c;
-      if (a_sk == 1) { r = e / kBK; c = e % kBK; } else { c = e / kBM; r = e % kBM; }
-      const int m = m0 + r, k = k0 + c;
-      As[r][c] = (m < M && k < kend) ? Au[(long)m * a_sm + (long)k * a_sk] : (uint16_t)0;
-    }
-    for (int e = tid; e < kBN * kBK; e += 128) {
-      int r, c;
-      if (b_sk == 1) { r = e / kBK; c = e % kBK; } else { c = e / kBN; r = e % kBN; }
-      const int n = n0 + r, k = k0 + c;
-      Bs[r][c] = (n < N && k < kend) ? Bu[(long)k * b_sk + (long)n * b_sn] : (uint16_t)0;
-    }
+    stage_tile(As, Au, a_sm, a_sk, m0, M, k0, kend, tid);
+    stage_tile(Bs, Bu, b_sn, b_sk, n0, N, k0, kend, tid);
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < kBK; kk += 16) {
