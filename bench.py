@@ -404,8 +404,10 @@ def main():
 
     tot_ms = 0.0
     fill_ms = 0.0
-    clock_path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                              else "_work", "bench_clocks_r%d.csv" % rank)
+    # raw nvidia-smi samples (TL_CLOCKS_DIR, default the temp directory)
+    import tempfile
+    clock_path = os.path.join(os.environ.get("TL_CLOCKS_DIR", tempfile.gettempdir()),
+                              "bench_clocks_r%d.csv" % rank)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()

@@ -1,7 +1,7 @@
 /*
  * lcirs_oracle.c - CPU restatement of TripleLens' LightCurveIRS path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker: tests/, the smoke check
+ * TEST INFRASTRUCTURE ONLY.  The oracle: tests/, the smoke check
  * and bench.py's CPU-baseline leg call it; the product never does.
  *
  * It restates, in plain C99, the algorithm of the reference files cited at

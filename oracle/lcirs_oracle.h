@@ -1,7 +1,7 @@
 /*
  * lcirs_oracle.h - CPU restatement of TripleLens' extended-source light-curve
- * path (LightCurveIRS), used ONLY as the checker by the tests, the smoke
- * check and the CPU-baseline leg of bench.py.  Nothing in the product links,
+ * path (LightCurveIRS): test infrastructure, used ONLY by the tests, the
+ * smoke check and the CPU-baseline leg of bench.py to check and time against.  Nothing in the product links,
  * loads or calls this library.
  *
  * Parity is pinned against the reference built from its own sources

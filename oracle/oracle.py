@@ -1,7 +1,7 @@
 """ctypes view of the C restatement of TripleLens' LightCurveIRS (the oracle).
 
 Test infrastructure only: tests/, ``__graft_entry__.smoke()`` and the CPU
-baseline leg of ``bench.py`` use it as the checker.  The product path never
+baseline leg of ``bench.py`` check and time against it.  The product path never
 imports this module.
 """
 import ctypes

@@ -1,0 +1,61 @@
+"""Host-side logic of the surrogate (no GPU): the parameter layout of the
+initialiser agrees with the FP64 restatement's, the sampler draws the
+configured distributions, and the training-row selection keeps only clean
+IRS labels away from the caustic."""
+import math
+import types
+
+import numpy as np
+
+
+def test_init_params_layout_matches_oracle():
+    from oracle import mlp
+    from triplelens_gb300 import surrogate as S
+    n = 16 * 256 + 256 + 3 * (256 * 256 + 256) + 256 + 1
+    p = S.init_params(np.random.default_rng(0), n)
+    layers, w5, b5 = mlp.unpack(p)
+    assert layers[0][0].shape == (256, 16)
+    assert np.all(layers[0][0][:, 14:] == 0.0)        # padding inputs
+    for w, b in layers:
+        assert np.all(b == 0.0) and np.std(w) > 0.0
+    assert w5.shape == (256,) and b5 == 0.0
+
+
+def test_sampler_distributions():
+    from triplelens_gb300 import surrogate as S
+    lenses, li, br, ix, off = S.sample_config5(3, 400, 16)
+    rho, v = lenses[:, 5], lenses[:, 6]
+    assert np.all((rho >= 1e-4) & (rho <= 3e-2))
+    assert abs(np.median(np.log10(rho)) - 0.5 * (-4 + math.log10(3e-2))) < 0.2
+    assert np.all((v >= 0.3) & (v <= 0.7)) and np.all(lenses[:, 7] == 500)
+    assert np.all((br >= 0) & (br < 6)) and np.all((ix >= 0) & (ix < 500))
+    r = np.hypot(off[:, 0], off[:, 1])
+    assert r.max() <= 3.0 and abs(np.median(r) - 3.0 / math.sqrt(2)) < 0.1   # uniform disc
+    _, li2, _, _, off2 = S.sample_config5(3, 400, 16, band=S.TRAIN_BAND)
+    d = np.hypot(off2[:, 0], off2[:, 1]) / lenses[li2, 5]
+    assert d.min() >= 2.0 * 0.999 and d.max() <= 10 ** 2.5 * 1.001
+
+
+def test_training_rows():
+    from triplelens_gb300 import surrogate as S
+
+    class T:
+        def __init__(self, a):
+            self.a = a
+
+        def cpu(self):
+            return self
+
+        def numpy(self):
+            return self.a
+
+    q = types.SimpleNamespace(
+        n=5,
+        irs=np.array([2.0, 2.0, 0.0, 3.0, 1.5]),
+        irs_status=np.array([0, 16, 0, 4, 0], np.uint32),
+        aps=T(np.array([1.9, 1.9, 1.0, 2.9, 1.4])),
+        dc=T(np.array([5.0, 5.0, 5.0, 5.0, 1.0], np.float32)))
+    y, ok = S.training_targets(q)
+    # clean, image-count warning kept; empty IRS, table-full and near-caustic dropped
+    assert list(ok) == [True, True, False, False, False]
+    assert abs(y[0] - math.log(2.0 / 1.9)) < 1e-6
