@@ -4,7 +4,7 @@ reference's golden fixtures.
 Parity levels:
   * given identical seed pixels, ray counts are bit-exact (every point);
   * seeds: the GPU's image solver follows the oracle's warm-start chain with
-    restarts every 8 points; seed sets are identical;
+    restarts every 4 points; seed sets are identical;
   * full pipeline vs the reference: identical on every point whose image
     decisions are not at the 1e-6 filter radius (the oracle flags those).
 Magnifications: exact for uniform sources (weights are exactly 1), within the
@@ -19,7 +19,7 @@ from triplelens_gb300 import workloads
 
 pytestmark = pytest.mark.gpu
 
-CHUNK = 8           # tl::kChainChunk
+CHUNK = 4           # tl::kChainChunk
 # weights are summed in FP32 per 32x8 tile and in 64-bit fixed point across
 # tiles; with limb darkening the magnification carries that rounding
 LD_RTOL_FP64 = 1e-6

@@ -19,7 +19,7 @@
 namespace tl {
 
 constexpr int kMaxSeeds = 64;     // seed pixels kept per point
-constexpr int kChainChunk = 8;    // points per warm-start chain (seed kernel)
+constexpr int kChainChunk = 4;    // points per warm-start chain (seed kernel)
 
 // status bits of a point (PointOut::status)
 enum : uint32_t {
