@@ -14,7 +14,9 @@ INCLUDE = os.path.join(ROOT, "include")
 
 REFERENCE_ABI = ["lcirs_new", "get_lc", "get_lc_irs", "copy_lc", "set_limb_darkening",
                  "set_amoeba_printout", "ccc_new", "get_cc", "get_ca", "print_ccc", "copy_cc_ca",
-                 "copy_lenses", "get_lens_pos", "get_bounding_box"]
+                 "copy_lenses", "get_lens_pos", "get_bounding_box", "img_new", "get_roots",
+                 "get_images", "set_pos", "copy_images", "lccuda_new", "get_lc_cuda",
+                 "set_limb_darkening_cuda"]
 
 
 def declared_functions(path):
@@ -51,7 +53,7 @@ def test_headers_declare_the_reference_abi():
 
 
 # header -> library that exports it
-LIBRARY_OF = {"ccc.h": "libccc.so"}
+LIBRARY_OF = {"ccc.h": "libccc.so", "img.h": "libimg.so", "lccuda.h": "liblccuda.so"}
 
 
 @pytest.mark.parametrize("header", [os.path.basename(h) for h in c_headers()])

@@ -321,3 +321,49 @@ def test_config4_graph_and_autotune(product_lib):
     b.run_device(3)
     _, cnt4, _ = b.download()
     assert np.array_equal(cnt3, cnt4)
+
+
+def test_img_abi_matches_reference(product_lib, golden_c1):
+    """libimg.so (img_new / get_images / copy_images) against the reference's
+    own img_* results for 64 source positions of the config-1 lens: the same
+    images (to 1e-9) flagged as images."""
+    import os as _os
+    from triplelens_gb300.img import Img
+    lens = golden_c1["lens"]
+    lib = _os.path.join(_os.path.dirname(product_lib), "libimg.so")
+    for k, (sx, sy) in enumerate(golden_c1["img_positions"]):
+        im = Img(*lens[:5], sx, sy, lib_path=lib)
+        im.get_images()
+        roots = np.zeros(10, np.cdouble)
+        flags = np.zeros(10, np.bool_)
+        im.copy_images(roots, flags)
+        mine = np.sort_complex(roots[flags])
+        ref = np.sort_complex(golden_c1["img_roots"][k][golden_c1["img_isimg"][k]])
+        assert len(mine) == len(ref), k
+        assert np.max(np.abs(mine - ref)) < 1e-9, k
+
+
+def test_lccuda_abi_routes_to_the_irs(product_lib):
+    """liblccuda.so: LC_cuda's get_lc_cuda gives the IRS curve of get_lc_irs,
+    get_lc the point-source curve of get_lc."""
+    import os as _os
+    from triplelens_gb300.img import LC_cuda
+    from triplelens_gb300.lcirs import LC_irs
+    lens, traj, n = workloads.config1()
+    lib = _os.path.join(_os.path.dirname(product_lib), "liblccuda.so")
+    a = LC_cuda(*lens[:5], lens[5], n, int(lens[7]), lib_path=lib)
+    a.lib_cuda.lcirs_set_verbose(a.obj, 0)
+    a.set_limb_darkening("linear", 0.5)
+    a.get_lc_cuda(*traj)
+    out_a = np.zeros(n)
+    a.copy_lc(out_a)
+    b = _lc(product_lib, np.r_[lens[:6], 0.5, lens[7]], n, 1)
+    b.get_lc_irs(*traj)
+    out_b = np.zeros(n)
+    b.copy_lc(out_b)
+    assert np.max(np.abs(out_a - out_b) / out_b) < LD_RTOL_SPLIT
+    a.get_lc(*traj)
+    b.get_lc(*traj)
+    a.copy_lc(out_a)
+    b.copy_lc(out_b)
+    assert np.max(np.abs(out_a - out_b) / np.abs(out_b)) < 1e-12

@@ -33,12 +33,17 @@ UNITS = [
     ("noalloc_abi.cu", []),
     ("surrogate.cu", []),
     ("ccc_abi.cu", ["--fmad=false"]),
+    ("img_abi.cu", ["--fmad=false"]),
+    ("lccuda_abi.cu", []),
 ]
 
 LIBS = {
     "liblcirs.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
                     "noalloc_abi.cu", "surrogate.cu"],
     "libccc.so": ["ccc_abi.cu"],
+    "libimg.so": ["img_abi.cu"],
+    "liblccuda.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
+                     "noalloc_abi.cu", "surrogate.cu", "lccuda_abi.cu"],
 }
 
 
