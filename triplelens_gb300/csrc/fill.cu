@@ -11,7 +11,8 @@
 //
 // Layout:
 //   * one CTA works on one source position at a time, taking positions from
-//     a global counter (persistent grid, two CTAs per SM);
+//     a size-ordered list, largest first (persistent grid, 2-4 CTAs per SM;
+//     the first CTAs own 4x larger tables and take the list's head);
 //   * per CTA a block table in HBM: 64-bit block keys (open addressing,
 //     linear probing, one CAS per probe) and block records holding the
 //     pending entry bits (seed rows, bottom row, top row, left and right
@@ -19,8 +20,9 @@
 //     accepted mask H (BH rows x 32 bits), the filled mask F and the F
 //     column summaries used to filter pushes;
 //   * per CTA a work ring of block slots; counters in shared memory.
-// A warp processes one block: lane = column, BH rays per lane; a ballot per
-// row builds the accepted masks; lane r < BH then holds row r, and the
+// A warp processes one block: lane = column, BH rays per lane, hits kept
+// as a per-lane column mask and turned into row masks by one ballot per row;
+// lane r < BH then holds row r, and the
 // closure of the entry bits is a bit-parallel run fill (carry propagation)
 // with shuffles between neighbouring rows; newly filled border bits are
 // pushed to the four neighbour blocks.  Closure distributes over union, so
