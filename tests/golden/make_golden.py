@@ -122,6 +122,43 @@ def ccc_worker(spec):
     np.savez(spec["out"], cc=cc, ca=ca, lenses=lz, box=box)
 
 
+def point_worker(spec):
+    """Child process: the reference's point-source curve (get_lc,
+    lcbase.cc:40-52) of one lens and trajectory."""
+    L = ctypes.cdll.LoadLibrary(spec["lib"])
+    d, vp = ctypes.c_double, ctypes.c_void_p
+    L.lcirs_new.argtypes = [d] * 6 + [ctypes.c_uint, ctypes.c_long]
+    L.lcirs_new.restype = vp
+    L.get_lc.argtypes = [vp] + [d] * 4
+    L.copy_lc.argtypes = [vp, vp]
+    a, b, th, m2, m3, rho, v, ppr = spec["lens"]
+    n = spec["n"]
+    o = L.lcirs_new(a, b, th, m2, m3, rho, n, int(ppr))
+    L.get_lc(o, *spec["traj"])
+    out = np.zeros(n)
+    L.copy_lc(o, out.ctypes.data_as(vp))
+    np.save(spec["out"], out)
+
+
+def point_fixtures(lib):
+    """Point-source curves of the config-1 lens and of three config-2 lenses."""
+    lens, traj, n = workloads.config1()
+    lenses, trajs, _ = workloads.config2(seed=11, n_curves=3)
+    cases = [(lens, traj, n)] + [(lenses[k], trajs[k], 500) for k in range(3)]
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for k, (L2, t, nn) in enumerate(cases):
+            spec = {"lib": lib, "lens": [float(x) for x in L2], "traj": [float(x) for x in t],
+                    "n": nn, "out": os.path.join(td, "p_%d.npy" % k)}
+            subprocess.run([sys.executable, __file__, "--point-worker", json.dumps(spec)],
+                           capture_output=True, text=True, check=True)
+            out["lens_%d" % k] = np.asarray(L2)
+            out["traj_%d" % k] = np.asarray(t)
+            out["amps_%d" % k] = np.load(spec["out"])
+    out["cases"] = np.array(len(cases))
+    return out
+
+
 def ccc_fixtures(lib):
     out = {"cases": np.array(CCC_CASES)}
     with tempfile.TemporaryDirectory() as td:
@@ -175,6 +212,7 @@ def main():
     ap.add_argument("--worker")
     ap.add_argument("--c2", action="store_true", help="also the 5000-point config-2 curve")
     ap.add_argument("--ccc-worker")
+    ap.add_argument("--point-worker")
     ap.add_argument("--only-ccc", action="store_true")
     args = ap.parse_args()
     if args.worker:
@@ -183,11 +221,16 @@ def main():
     if args.ccc_worker:
         ccc_worker(json.loads(args.ccc_worker))
         return
+    if args.point_worker:
+        point_worker(json.loads(args.point_worker))
+        return
     subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", "REF=" + args.ref], cwd=ROOT,
                    check=True)
 
     np.savez_compressed(os.path.join(HERE, "ccc.npz"), **ccc_fixtures(REF_LIBS["fast"]))
     print("wrote ccc.npz")
+    np.savez_compressed(os.path.join(HERE, "point_lc.npz"), **point_fixtures(REF_LIBS["nfc"]))
+    print("wrote point_lc.npz")
     if args.only_ccc:
         return
 

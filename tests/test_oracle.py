@@ -149,3 +149,18 @@ def test_reference_build_spread_is_small():
         a = z["counts_%d" % k].astype(np.int64)
         b = z["counts_fast_%d" % k].astype(np.int64)
         assert np.max(np.abs(a - b)) <= 64
+
+
+def test_point_source_curves_match_reference(oracle_lib):
+    """Point-source curves (get_lc, lcbase.cc:40-52) against the reference
+    built without FMA contraction (tests/golden/point_lc.npz): the config-1
+    lens to 1e-9; config-2 lenses, whose small-mass lenses make single image
+    magnifications rounding-sensitive, to 1e-4 (the reference's own -Ofast
+    build differs from that build by up to 45 % at single points)."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "point_lc.npz"))
+    for k in range(int(z["cases"])):
+        L, t, ref = z["lens_%d" % k], z["traj_%d" % k], z["amps_%d" % k]
+        o = oracle_lib.OracleIRS(*L[:5], L[5], len(ref), int(L[7]))
+        o.set_chain_chunk(0)
+        rel = np.abs(o.lc_point(*t) - ref) / ref
+        assert rel.max() < (1e-9 if k == 0 else 1e-4), (k, rel.max())
