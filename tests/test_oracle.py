@@ -1,6 +1,8 @@
 """The oracle (C restatement, oracle/lcirs_oracle.c) against the reference's
 own known answers: the Laguerre tests of tests/laguerretest.cc and golden
 fixtures produced by the reference build (tests/golden/make_golden.py)."""
+import os
+
 import numpy as np
 import pytest
 
