@@ -172,6 +172,18 @@ def measured_peaks():
     return {}
 
 
+def hbm_view(traffic_bytes, fill_s, peaks):
+    """The fill's DRAM traffic per launch (from the ncu calibration) as a
+    bandwidth against the measured HBM copy peak: how far the kernel is from
+    being memory-bound."""
+    peak = peaks.get("hbm_gbs") or 6800.0
+    if not traffic_bytes or not fill_s or fill_s <= 0:
+        return None
+    gbs = traffic_bytes / fill_s / 1e9
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": "MEASURED_PEAKS hbm_gbs" if peaks.get("hbm_gbs") else "fallback"}
+
+
 # ---------------------------------------------------------------------------
 def config4_leg(seed, curves, reps):
     """Config 4 (sub-sample): `curves` light curves of 2000 points, each its
@@ -487,7 +499,8 @@ def main():
                      "flop_per_ray": FLOP_PER_RAY, "flop_per_accepted_ray": FLOP_PER_WEIGHT,
                      "peak_source": "2 x 128 FP32 lanes x %d SMs x sm_max_mhz %.0f (MEASURED_PEAKS)"
                                     % (sms, sm_max),
-                     "fill_ms_per_step": fill_ms / args.steps},
+                     "fill_ms_per_step": fill_ms / args.steps,
+                     "hbm_view": hbm_view(traffic, fill_s, peaks)},
         "rays": {"accepted_per_step": int(stats[3]), "evaluated_per_step": int(stats[0]),
                  "fp64_per_step": int(stats[1]), "tiles_per_step": int(stats[2]),
                  "accepted_per_s": float(stats[3]) * world / (ms_step / 1e3),

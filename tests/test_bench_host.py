@@ -1,0 +1,30 @@
+"""bench.py host-side helpers (no GPU): the HBM view of the fill's DRAM
+traffic and the reference arm's JSON line shape."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_hbm_view():
+    import bench
+    v = bench.hbm_view(2.0e11, 0.5, {"hbm_gbs": 8000.0})
+    assert abs(v["achieved"] - 400.0) < 1e-9 and abs(v["frac"] - 0.05) < 1e-12
+    assert v["peak_source"].startswith("MEASURED")
+    assert bench.hbm_view(None, 0.5, {}) is None
+    assert bench.hbm_view(1.0, 0.0, {}) is None
+
+
+def test_reference_arm_prints_one_json_line():
+    """`bench.py --impl reference` (the oracle on the host cores) prints the
+    contract's line with impl, cpu_baseline and e2e."""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0", "--cpu-sample", "16"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "points/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
