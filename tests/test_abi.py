@@ -78,3 +78,25 @@ def test_product_path_has_no_oracle_dependency():
                     text = fh.read()
                 assert "import oracle" not in text and "from oracle" not in text, f
                 assert "liboracle" not in text, f
+
+
+def test_entry_points_reject_bad_arguments_without_a_gpu(product_lib):
+    """Argument errors return their documented codes before any CUDA call
+    (include/tl_batch.h, include/lcirs.h, include/tl_surrogate.h)."""
+    lib = ctypes.CDLL(product_lib)
+    vp = ctypes.c_void_p
+    f = lib.lcirs_fill_device_noalloc
+    f.argtypes = [vp, ctypes.c_int] + [vp] * 7
+    f.restype = ctypes.c_int
+    assert f(None, 10, None, None, None, None, None, None, None) == -1
+    for name, args in (("tlb_run_device", [None, 3, None]), ("tlb_stats", [None, None]),
+                       ("tlb_graph_launch", [None, None]), ("tlb_graph_capture", [None])):
+        fn = getattr(lib, name)
+        fn.restype = ctypes.c_int
+        fn.argtypes = [vp if not isinstance(a, int) else ctypes.c_int for a in args]
+        assert fn(*args) == -1, name
+    fn = lib.tls_predict
+    fn.restype = ctypes.c_int
+    assert fn(None, 0, None, None, None, ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0),
+              None, None, None, None, None) == -1
+    assert lib.tls_param_count() == 16 * 256 + 256 + 3 * (256 * 256 + 256) + 256 + 1
