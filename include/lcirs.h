@@ -99,6 +99,16 @@ void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3);
  * tile-relative map with an FP64 guard band at the limb (default). */
 void lcirs_set_precision(LightCurveIRS* lc, int mode);
 
+/* Warm-start chain of the image solver.  0 (default): one chain carried
+ * through every get_lc_irs / get_lc call of the object, as the reference's
+ * ImgPoint member carries it (imgpoint.cc:160-205) - ray counts equal the
+ * reference's (strict IEEE build) on every point, and the chain runs serially
+ * on the GPU.  k > 0: the chain restarts from the constructor's state every
+ * k points and chunks run in parallel; counts then differ from the
+ * reference's at the few points whose image decisions depend on the last
+ * bits of the warm start. */
+void lcirs_set_chain(LightCurveIRS* lc, int points);
+
 /* Fill-kernel diagnostics of the last get_lc_irs, n+1 entries: bits 0-15
  * the largest number of passes over one tile, bit 16 pass limit reached,
  * bit 17 dequeue limit reached, bits 24-31 the tile state seen then. */

@@ -36,6 +36,9 @@ struct LightCurveIRS {
   unsigned int lastStatus = 0;
   int verbose = 1;
   int precision = 1;
+  // warm-start chain of the image solver: 0 = one chain carried over the
+  // object's life (the reference), k > 0 = restart every k points
+  int chainPoints = 0;
 
   // lens and grid (host copies)
   double a, b, th, m1, m2, m3;

@@ -66,6 +66,16 @@ int tlb_stats(tl_batch* b, uint64_t* out4);
 int tlb_configure(tl_batch* b, int precision, int fill_ctas, int table_log2, int threads,
                   int block_h);
 
+/* Warm-start chain of the image solver.  points > 0: the chain restarts
+ * from the lens's construction state every `points` points of a curve, so
+ * chunks of a curve run in parallel (default 4); the result is the one the
+ * reference would give with the same restarts, and it differs from the
+ * reference's single chain at points whose image decisions depend on the
+ * last bits of the warm start.  points <= 0: one chain per curve, the
+ * reference's order, bit-exact with it on every point (serial per curve).
+ * Takes effect at the next tlb_set_trajectories. */
+int tlb_set_chain(tl_batch* b, int points);
+
 /* Point-source magnifications (reference get_lc sampling t = i/(n-1)) of the
  * current trajectories, n points each, written to amp (host). */
 long tlb_point_lc(tl_batch* b, double* amp);

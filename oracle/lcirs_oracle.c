@@ -13,6 +13,7 @@
  */
 #include "lcirs_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -23,8 +24,20 @@
 #endif
 
 /* ------------------------------------------------------------------------ */
-/* complex arithmetic (std::complex<double> semantics under the reference's  */
-/* -Ofast build: naive division, |z| = sqrt(re^2 + im^2))                    */
+/* complex arithmetic with the semantics std::complex<double> has in a       */
+/* strict IEEE build (g++ -O2 -fno-fast-math -ffp-contract=off):             */
+/*   a * b   the textbook product (the library's NaN recovery never applies  */
+/*           to the finite values of this path);                             */
+/*   a / b   Smith's algorithm (R. L. Smith, "Algorithm 116: Complex         */
+/*           division", CACM 5(8), 1962), the method of libgcc's __divdc3;   */
+/*   |a|     hypot, computed as in C. F. Borges, "An improved algorithm for  */
+/*           hypot(a,b)", 2019 (arXiv:1904.09481): a naive square root       */
+/*           corrected by the exactly re-expressed residual, the no-FMA form;*/
+/*   sqrt(a) the half-angle principal root built on that hypot (W. Kahan,    */
+/*           "Branch cuts for complex elementary functions", 1987).         */
+/* Each agrees bit for bit with glibc's hypot/csqrt and libgcc's division   */
+/* (checked on 2e7 random operands), so the oracle rounds exactly as the    */
+/* reference's strict build does.                                            */
 /* ------------------------------------------------------------------------ */
 typedef struct { double re, im; } cx;
 
@@ -38,21 +51,63 @@ static inline cx cmul(cx a, cx b) {
 }
 static inline cx cscale(cx a, double s) { return mk(a.re * s, a.im * s); }
 static inline cx cdiv(cx a, cx b) {
-  double d = b.re * b.re + b.im * b.im;
-  return mk((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+  if (fabs(b.re) < fabs(b.im)) {
+    double r = b.re / b.im, den = b.re * r + b.im;
+    if (fabs(r) > DBL_MIN) return mk((a.re * r + a.im) / den, (a.im * r - a.re) / den);
+    return mk((b.re * (a.re / b.im) + a.im) / den, (b.re * (a.im / b.im) - a.re) / den);
+  }
+  double r = b.im / b.re, den = b.im * r + b.re;
+  if (fabs(r) > DBL_MIN) return mk((a.im * r + a.re) / den, (a.im - a.re * r) / den);
+  return mk((a.re + b.im * (a.im / b.re)) / den, (a.im - b.im * (a.re / b.re)) / den);
 }
 /* real / complex, as complex<double>(x) /= y */
 static inline cx rdiv(double x, cx b) { return cdiv(mk(x, 0.0), b); }
 static inline double cnorm(cx a) { return a.re * a.re + a.im * a.im; }
-static inline double cabs_(cx a) { return sqrt(a.re * a.re + a.im * a.im); }
-/* principal square root, half-angle form t = sqrt((|x| + |z|)/2).  The
- * reference calls libm's csqrt (std::sqrt(complex)); both give the principal
- * root, and agree to rounding. */
-static inline cx csqrt_(cx a) {
-  if (a.re == 0.0 && a.im == 0.0) return mk(0.0, a.im);
-  double t = sqrt((fabs(a.re) + cabs_(a)) * 0.5);
-  if (a.re >= 0.0) return mk(t, a.im / (2.0 * t));
-  return mk(fabs(a.im) / (2.0 * t), a.im < 0.0 ? -t : t);
+static double hypot_kernel(double ax, double ay) {
+  double h = sqrt(ax * ax + ay * ay), t1, t2;
+  if (h <= 2.0 * ay) {
+    double d = h - ay;
+    t1 = ax * (2.0 * d - ax);
+    t2 = (d - 2.0 * (ax - ay)) * d;
+  } else {
+    double d = h - ax;
+    t1 = 2.0 * d * (ax - 2.0 * ay);
+    t2 = (4.0 * d - ay) * ay + d * d;
+  }
+  return h - (t1 + t2) / (2.0 * h);
+}
+static double hypot_(double x, double y) {
+  x = fabs(x);
+  y = fabs(y);
+  double ax = x < y ? y : x, ay = x < y ? x : y;
+  if (ax > 0x1p+511) {
+    if (ay <= ax * 0x1p-54) return ax + ay;
+    return hypot_kernel(ax * 0x1p-600, ay * 0x1p-600) / 0x1p-600;
+  }
+  if (ay < 0x1p-511) {
+    if (ax >= ay / 0x1p-54) return ax + ay;
+    return hypot_kernel(ax / 0x1p-600, ay / 0x1p-600) * 0x1p-600;
+  }
+  if (ay <= ax * 0x1p-54) return ax + ay;
+  return hypot_kernel(ax, ay);
+}
+static inline double cabs_(cx a) { return hypot_(a.re, a.im); }
+static cx csqrt_(cx a) {
+  if (a.im == 0.0) {
+    if (a.re < 0.0) return mk(0.0, copysign(sqrt(-a.re), a.im));
+    return mk(fabs(sqrt(a.re)), copysign(0.0, a.im));
+  }
+  if (a.re == 0.0) {
+    double r = sqrt(0.5 * fabs(a.im));
+    return mk(r, copysign(r, a.im));
+  }
+  double d = hypot_(a.re, a.im);
+  if (a.re > 0.0) {
+    double r = sqrt(0.5 * (d + a.re));
+    return mk(r, 0.5 * (a.im / r));
+  }
+  double s = sqrt(0.5 * (d - a.re));
+  return mk(fabs(0.5 * (a.im / s)), copysign(s, a.im));
 }
 
 /* ------------------------------------------------------------------------ */
@@ -184,6 +239,25 @@ struct orc_lcirs {
   /* ImgPoint warm-start state (imgpoint.h:104-110) */
   cx temp_roots[11];
   int have_temp;
+  /* zeta-free coefficients, computed once per object (imgpoint.cc:164-168) */
+  cx coef_nozeta[11];
+  /* Model of the heap memory the warm start reads (quirk Q4).  The reference
+   * starts root 10 of a warm solve from _tempRoots[10], one element past the
+   * end of a 10-element vector whose buffer has capacity 16 (256 bytes).  That
+   * slot holds whatever the chunk held before: glibc serves 256-byte requests
+   * from a per-thread LIFO cache of freed chunks (tcache), and the only
+   * 256-byte buffers on this path are vectors of capacity 16 - the roots
+   * vectors, the image list of a point with 9+ seeds, the ImgPoint image list
+   * with 9+ images, and, during construction, the critical-curve branches
+   * growing past 16 samples.  heap[] holds the slot-10 contents of the cached
+   * chunks (top last); temp_slot is the slot of the chunk _tempRoots holds. */
+  cx heap[8];     /* the path never caches more than 5 */
+  int heap_n;
+  cx temp_slot;
+  int have_temp_chunk;
+  int imgs_big;   /* the ImgPoint image list has grown to capacity 16 */
+  double *trace;  /* optional record of the slot read by each warm solve */
+  long trace_cap, trace_n;
   int chain_chunk; /* 0: one warm-start chain (reference); K: restart every K points */
   int fragile;     /* set when an image decision sat near the filter radius */
   double fragile_band; /* residual below which a filter/lens-equation
@@ -315,55 +389,28 @@ static void get_img_plane_pars(orc_lcirs *o) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Degree-10 lens polynomial.                                                */
-/* Own derivation (algebraically equal to imgpointcoeff.cc:223-447 up to a   */
-/* constant factor): with Q = prod(z - z_k), P = sum m_i prod_{k!=i}(z-z_k), */
-/* R_i = (conj(zeta) - conj(z_i)) Q + P, the lens equation becomes           */
-/*   (z - zeta) R1 R2 R3 - Q (m1 R2 R3 + m2 R1 R3 + m3 R1 R2) = 0.           */
+/* Degree-10 lens polynomial: imgpoint.cc:160-176 adds the cached zeta-free  */
+/* part (imgpointcoeff.cc:223-278) and the zeta part (:280-447) term by      */
+/* term.  Both expression trees live in lens_coeffs.c, in the reference's   */
+/* evaluation order.                                                         */
 /* ------------------------------------------------------------------------ */
-static void pmul(const cx *a, int da, const cx *b, int db, cx *out) {
-  for (int i = 0; i <= da + db; i++) out[i] = mk(0.0, 0.0);
-  for (int i = 0; i <= da; i++)
-    for (int j = 0; j <= db; j++) out[i + j] = cadd(out[i + j], cmul(a[i], b[j]));
+void orc_coeffs_nozeta(double m2, double m3, const double z2xy[2], const double z3xy[2],
+                       double _Complex out[11]);
+void orc_coeffs_zeta(double m2, double m3, const double z2xy[2], const double z3xy[2],
+                     double zx, double zy, double _Complex out[11]);
+
+static void lens_poly_init(orc_lcirs *o) {
+  double _Complex c[11];
+  const double z2[2] = {o->z2.re, o->z2.im}, z3[2] = {o->z3.re, o->z3.im};
+  orc_coeffs_nozeta(o->m2, o->m3, z2, z3, c);
+  for (int k = 0; k < 11; k++) o->coef_nozeta[k] = mk(__real__ c[k], __imag__ c[k]);
 }
 
 static void lens_poly(const orc_lcirs *o, cx zeta, cx *c /* 11 */) {
-  const cx zs[3] = {o->z1, o->z2, o->z3};
-  const double ms[3] = {o->m1, o->m2, o->m3};
-  cx l[3][2];
-  for (int k = 0; k < 3; k++) { l[k][0] = cneg(zs[k]); l[k][1] = mk(1.0, 0.0); }
-  cx q2[3], Q[4];
-  pmul(l[0], 1, l[1], 1, q2);
-  pmul(q2, 2, l[2], 1, Q);
-  cx P[3] = {mk(0, 0), mk(0, 0), mk(0, 0)};
-  for (int i = 0; i < 3; i++) {
-    cx t[3];
-    pmul(l[(i + 1) % 3], 1, l[(i + 2) % 3], 1, t);
-    for (int d = 0; d < 3; d++) P[d] = cadd(P[d], cscale(t[d], ms[i]));
-  }
-  cx R[3][4];
-  cx zc = cconj(zeta);
-  for (int i = 0; i < 3; i++) {
-    cx f = csub(zc, cconj(zs[i]));
-    for (int d = 0; d < 4; d++) R[i][d] = cmul(f, Q[d]);
-    for (int d = 0; d < 3; d++) R[i][d] = cadd(R[i][d], P[d]);
-  }
-  cx r12[7], r13[7], r23[7], r123[10];
-  pmul(R[0], 3, R[1], 3, r12);
-  pmul(R[0], 3, R[2], 3, r13);
-  pmul(R[1], 3, R[2], 3, r23);
-  pmul(r12, 6, R[2], 3, r123);
-  cx zl[2] = {cneg(zeta), mk(1.0, 0.0)};
-  cx lhs[11];
-  pmul(zl, 1, r123, 9, lhs);
-  cx s[7];
-  for (int d = 0; d < 7; d++)
-    s[d] = cadd(cadd(cscale(r23[d], ms[0]), cscale(r13[d], ms[1])),
-                cscale(r12[d], ms[2]));
-  cx rhs[10];
-  pmul(Q, 3, s, 6, rhs);
-  for (int d = 0; d < 11; d++) c[d] = lhs[d];
-  for (int d = 0; d < 10; d++) c[d] = csub(c[d], rhs[d]);
+  double _Complex d[11];
+  const double z2[2] = {o->z2.re, o->z2.im}, z3[2] = {o->z3.re, o->z3.im};
+  orc_coeffs_zeta(o->m2, o->m3, z2, z3, zeta.re, zeta.im, d);
+  for (int k = 0; k < 11; k++) c[k] = cadd(o->coef_nozeta[k], mk(__real__ d[k], __imag__ d[k]));
 }
 
 /* imgpoint.cc:72-90 */
@@ -374,18 +421,46 @@ static int img_check(const orc_lcirs *o, cx img, cx src, double radius) {
   return cabs_(csub(t, src)) < radius;
 }
 
+/* tcache model: a 256-byte request takes the most recently freed chunk */
+static cx heap_pop(orc_lcirs *o) {
+  if (o->heap_n > 0) return o->heap[--o->heap_n];
+  return mk(0.0, 0.0); /* a chunk carved from fresh memory */
+}
+static void heap_push(orc_lcirs *o, cx slot) {
+  if (o->heap_n < 8) o->heap[o->heap_n++] = slot;
+}
+/* _tempRoots = <new roots vector>: the solver's result vector took a chunk
+ * (pushed to capacity 16 by its 9th root), then the old buffer is freed. */
+static void temp_roots_replaced(orc_lcirs *o) {
+  cx v = heap_pop(o);
+  if (o->have_temp_chunk) heap_push(o, o->temp_slot);
+  o->temp_slot = v;
+  o->have_temp_chunk = 1;
+}
+
 /* imgpoint.cc:160-205 */
 static void get_roots_precalculated(orc_lcirs *o, cx zeta, int force, cx *roots) {
   cx c[11];
   lens_poly(o, zeta, c);
   if (!o->have_temp || force) {
     solve_roots(c, 10, NULL, o->temp_roots);
+    temp_roots_replaced(o);
     o->have_temp = 1;
   } else {
     cx fresh[10];
+    o->temp_roots[10] = o->temp_slot;
+    if (o->trace && o->trace_n < o->trace_cap) {
+      o->trace[2 * o->trace_n] = o->temp_slot.re;
+      o->trace[2 * o->trace_n + 1] = o->temp_slot.im;
+      o->trace_n++;
+    }
     solve_roots(c, 10, o->temp_roots, fresh);
     memcpy(o->temp_roots, fresh, sizeof(fresh));
-    if (!check_roots(c, 10, o->temp_roots)) solve_roots(c, 10, NULL, o->temp_roots);
+    temp_roots_replaced(o);
+    if (!check_roots(c, 10, o->temp_roots)) {
+      solve_roots(c, 10, NULL, o->temp_roots);
+      temp_roots_replaced(o);
+    }
   }
   memcpy(roots, o->temp_roots, 10 * sizeof(cx));
 }
@@ -426,7 +501,15 @@ static int filter_images(orc_lcirs *o, const cx *roots, cx zeta, cx *imgs) {
   int n = 0;
   for (int k = 0; k < 10; k++) {
     int accepted = img_check(o, roots[k], zeta, 1.0e-6);
-    if (accepted) imgs[n++] = roots[k];
+    if (accepted) {
+      imgs[n++] = roots[k];
+      /* the ImgPoint image list outgrows capacity 8 once and keeps its
+       * 256-byte buffer for the life of the object */
+      if (n == 9 && !o->imgs_big) {
+        heap_pop(o);
+        o->imgs_big = 1;
+      }
+    }
     /* The image set depends on rounding when a residual sits within a decade
      * of the 1e-6 filter radius (double roots at caustic points), or when
      * the filter's verdict disagrees with the lens equation itself (roots
@@ -755,11 +838,43 @@ static int intersection_check(const orc_lcirs *o, cx src, cx A, cx B, cx *trial)
   return 0;
 }
 
+static void heap_construction_state(orc_lcirs *o) {
+  /* Construction leaves five 256-byte chunks in the cache: each critical-
+   * curve branch vector outgrows capacity 16 at sample 16 (ccc.cc:88-95,
+   * branches in order) and frees a buffer whose slot 10 is sample 10 of that
+   * branch; branch 5's chunk is taken again by the caustic branches and the
+   * caustic boxes (lcirs.cc:39-48).  Verified on the reference build. */
+  o->heap_n = 0;
+  for (int k = 0; k < 5; k++) heap_push(o, o->cc[k][10]);
+  o->have_temp_chunk = 0;
+  o->temp_slot = mk(0.0, 0.0);
+  o->imgs_big = 0;
+}
+
+/* The point's seed list imgPos (lcirs.cc:123) starts as a copy of the
+ * image list, capacity = size, and doubles when full (libstdc++).  Its
+ * 256-byte stage (capacity 16) takes a cached chunk and gives it back when it
+ * grows again or when the point ends; slot 10 then holds seed 10. */
+typedef struct { int size, cap; cx slot; } seed_list;
+
+static void seed_list_push(orc_lcirs *o, seed_list *l, cx z) {
+  if (l->size == l->cap) {
+    int nc = l->cap ? 2 * l->cap : 1;
+    cx slot = l->slot;
+    if (nc == 16) l->slot = heap_pop(o);
+    if (l->cap == 16) heap_push(o, slot);
+    l->cap = nc;
+  }
+  if (l->size == 10 && l->cap == 16) l->slot = z;
+  l->size++;
+}
+
 /* seeds of one point, lcirs.cc:123-165; returns the number of seeds */
 static int point_seeds(orc_lcirs *o, cx pos, cx *seeds, int cap) {
   cx imgs[10];
   int n = get_images(o, pos, imgs);
   int ns = 0;
+  seed_list sl = {n, n, mk(0.0, 0.0)};
   for (int k = 0; k < n; k++)
     if (ns < cap) seeds[ns++] = imgs[k];
   for (int k = 0; k < NBR; k++) {
@@ -771,8 +886,10 @@ static int point_seeds(orc_lcirs *o, cx pos, cx *seeds, int cap) {
         if (intersection_check(o, pos, o->ca[k][j], o->ca[k][j + 1], &trial)) {
           if (!taken) {
             int m = get_images(o, trial, imgs);
-            for (int q = 0; q < m; q++)
+            for (int q = 0; q < m; q++) {
+              seed_list_push(o, &sl, imgs[q]);
               if (ns < cap) seeds[ns++] = imgs[q];
+            }
             taken = 1;
           }
         } else {
@@ -781,6 +898,7 @@ static int point_seeds(orc_lcirs *o, cx pos, cx *seeds, int cap) {
       }
     }
   }
+  if (sl.cap == 16) heap_push(o, sl.slot);
   return ns;
 }
 
@@ -811,8 +929,18 @@ orc_lcirs *orc_new(double a, double b, double th, double m2, double m3,
   get_ca(o);
   get_ca_boxes(o);
   get_img_plane_pars(o);
+  lens_poly_init(o);
+  heap_construction_state(o);
   return o;
 }
+
+/* Record the slot-10 value each warm solve starts root 10 from. */
+void orc_set_trace(orc_lcirs *o, double *buf, long cap) {
+  o->trace = buf;
+  o->trace_cap = cap;
+  o->trace_n = 0;
+}
+long orc_trace_count(const orc_lcirs *o) { return o->trace_n; }
 
 void orc_free(orc_lcirs *o) {
   if (!o) return;
@@ -856,8 +984,13 @@ void orc_ld(const orc_lcirs *o, double *A, double *B, double *intensity) {
  * the object (imgpoint.cc:184-198).  With chain_chunk = K > 0 the chain is
  * restarted cold at every point index that is a multiple of K, which is how
  * the GPU engine splits a trajectory into independent chunks. */
+/* A restart returns the solver to the state the constructor leaves: no
+ * roots, and the constructor's cache of freed chunks. */
 static inline void chain_restart(orc_lcirs *o, unsigned i) {
-  if (o->chain_chunk > 0 && i % (unsigned)o->chain_chunk == 0) o->have_temp = 0;
+  if (o->chain_chunk > 0 && i % (unsigned)o->chain_chunk == 0) {
+    o->have_temp = 0;
+    heap_construction_state(o);
+  }
 }
 
 void orc_set_chain_chunk(orc_lcirs *o, int k) { o->chain_chunk = k; }
@@ -995,6 +1128,7 @@ int orc_images_cold(double a, double b, double th, double m2, double m3,
   o.z2 = mk(a, 0.0);
   o.z3 = mk(b * cos(th), b * sin(th));
   o.is_binary_img = (a == 0.0 || b == 0.0 || m3 == 0.0);
+  lens_poly_init(&o);
   cx imgs[10];
   int n = get_images(&o, mk(sx, sy), imgs);
   for (int k = 0; k < n; k++) {

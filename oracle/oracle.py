@@ -59,6 +59,9 @@ def lib():
         L.orc_laguerre.argtypes = [dp, ctypes.c_int, dp]
         L.orc_laguerre.restype = ctypes.c_int
         L.orc_lens_poly.argtypes = [vp, d, d, dp]
+        L.orc_set_trace.argtypes = [vp, dp, ctypes.c_long]
+        L.orc_trace_count.argtypes = [vp]
+        L.orc_trace_count.restype = ctypes.c_long
         _lib = L
     return _lib
 
@@ -114,6 +117,16 @@ class OracleIRS:
     def set_chain_chunk(self, k):
         """Restart the warm-start chain every k points (0: one chain)."""
         self.L.orc_set_chain_chunk(self.obj, int(k))
+
+    def trace_slots(self, cap):
+        """Record the value each warm solve starts root 10 from (the heap
+        slot the reference reads past the end of its root vector)."""
+        self._trace = np.zeros(2 * cap)
+        self.L.orc_set_trace(self.obj, _p(self._trace), cap)
+
+    def traced_slots(self):
+        n = self.L.orc_trace_count(self.obj)
+        return self._trace[0:2 * n:2] + 1j * self._trace[1:2 * n:2]
 
     def set_fragile_band(self, r):
         self.L.orc_set_fragile_band(self.obj, float(r))

@@ -8,10 +8,17 @@ Ray counts are read from the reference's per-point stdout line
 "irs amplification: A and the count N ..." (lcirs.cc:176-177); the filled
 sets from its amoeba dump files (amoeba.cc:90-108).
 
-    python tests/golden/make_golden.py [--ref /path/to/TripleLens] [--c2]
+Three reference builds (oracle/Makefile.ref): "strict" (IEEE, -O2
+-fno-fast-math -ffp-contract=off), the pinned parity target; "nfc" and
+"fast", the makefile's -Ofast flags without and with FMA contraction, kept to
+show the reference's own build-to-build spread.
 
-Each reference run happens in a child process (its stdout is C++ cout).
-The committed outputs are small .npz files; this script is kept beside them.
+    python tests/golden/make_golden.py --ref <TripleLens checkout> [--c2] [--bench]
+
+(--ref may be replaced by TRIPLELENS_REF in the environment.)  Each reference
+run happens in a child process of its own (its stdout is C++ cout, and its
+warm start depends on the process's heap history), several at a time.  The
+committed outputs are small .npz files; this script is kept beside them.
 """
 import argparse
 import ctypes
@@ -21,6 +28,7 @@ import re
 import subprocess
 import sys
 import tempfile
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -31,9 +39,11 @@ sys.path.insert(0, ROOT)
 from triplelens_gb300 import workloads  # noqa: E402
 
 REF_LIBS = {
+    "strict": os.path.join(ROOT, "oracle", "_ref", "liblcirs_ref_strict.so"),
     "nfc": os.path.join(ROOT, "oracle", "_ref", "liblcirs_ref_nfc.so"),
     "fast": os.path.join(ROOT, "oracle", "_ref", "liblcirs_ref.so"),
 }
+POOL = ThreadPoolExecutor(max_workers=os.cpu_count() or 4)
 
 
 def worker(spec):
@@ -62,12 +72,24 @@ def worker(spec):
     np.save(spec["amp_out"], out)
 
 
+def _big_stack():
+    import resource
+    soft, hard = resource.getrlimit(resource.RLIMIT_STACK)
+    want = 1 << 33
+    if hard != resource.RLIM_INFINITY:
+        want = min(want, hard)
+    resource.setrlimit(resource.RLIMIT_STACK, (want, hard))
+
+
 def run_curve(lib, lens, traj, n, amoeba=None):
     with tempfile.TemporaryDirectory() as td:
         spec = {"lib": lib, "lens": [float(x) for x in lens], "traj": [float(x) for x in traj],
                 "n": int(n), "amp_out": os.path.join(td, "amp.npy"), "amoeba": amoeba}
+        # the reference's flood fill recurses once per filled row
+        # (lcirs.cc:446-463): the largest images need more than the default
+        # 8 MiB of stack
         r = subprocess.run([sys.executable, __file__, "--worker", json.dumps(spec)],
-                           capture_output=True, text=True, check=True)
+                           capture_output=True, text=True, check=True, preexec_fn=_big_stack)
         counts = np.array([int(m) for m in re.findall(r"the count (\d+)", r.stdout)], np.uint64)
         amps = np.load(spec["amp_out"])
     assert len(counts) == n + 1, (len(counts), n)
@@ -206,14 +228,24 @@ def ccc_and_images(lib, lens, positions):
     return cc, ca, roots, isimg
 
 
+def curves(lib, lenses, trajs, n):
+    """Reference curves, several child processes at a time."""
+    futs = [POOL.submit(run_curve, lib, lenses[k], trajs[k], n) for k in range(len(lenses))]
+    return [f.result() for f in futs]
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("TRIPLELENS_REF"))
     ap.add_argument("--worker")
     ap.add_argument("--c2", action="store_true", help="also the 5000-point config-2 curve")
+    ap.add_argument("--bench", action="store_true",
+                    help="also the benchmark's 8 curves (seed 2024, strict build only)")
     ap.add_argument("--ccc-worker")
     ap.add_argument("--point-worker")
     ap.add_argument("--only-ccc", action="store_true")
+    ap.add_argument("--only-bench", action="store_true",
+                    help="only the benchmark fixture (implies --bench)")
     args = ap.parse_args()
     if args.worker:
         worker(json.loads(args.worker))
@@ -224,29 +256,36 @@ def main():
     if args.point_worker:
         point_worker(json.loads(args.point_worker))
         return
+    if not args.ref:
+        ap.error("give --ref <TripleLens checkout> or set TRIPLELENS_REF")
     subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", "REF=" + args.ref], cwd=ROOT,
                    check=True)
 
+    if args.only_bench:
+        args.bench = True
+        bench_fixture()
+        return
     np.savez_compressed(os.path.join(HERE, "ccc.npz"), **ccc_fixtures(REF_LIBS["fast"]))
     print("wrote ccc.npz")
-    np.savez_compressed(os.path.join(HERE, "point_lc.npz"), **point_fixtures(REF_LIBS["nfc"]))
+    np.savez_compressed(os.path.join(HERE, "point_lc.npz"), **point_fixtures(REF_LIBS["strict"]))
     print("wrote point_lc.npz")
     if args.only_ccc:
         return
 
     lens, traj, n = workloads.config1()
     out = {"lens": lens, "traj": traj, "n": n}
+    jobs = {}
     for tag, v in (("uniform", 0.0), ("default", -1.0), ("linear05", 0.5)):
         L2 = lens.copy()
         L2[6] = v
         for build, lib in REF_LIBS.items():
-            c, a = run_curve(lib, L2, traj, n)
-            out["counts_%s_%s" % (tag, build)] = c
-            out["amps_%s_%s" % (tag, build)] = a
+            jobs[(tag, build)] = POOL.submit(run_curve, lib, L2, traj, n)
+    for (tag, build), f in jobs.items():
+        out["counts_%s_%s" % (tag, build)], out["amps_%s_%s" % (tag, build)] = f.result()
     with tempfile.TemporaryDirectory() as td:
         L2 = lens.copy()
         L2[6] = 0.0
-        run_curve(REF_LIBS["nfc"], L2, traj, n, amoeba=os.path.join(td, "amo_"))
+        run_curve(REF_LIBS["strict"], L2, traj, n, amoeba=os.path.join(td, "amo_"))
         pts = [0, 20, 50, 75, 100]
         out["amoeba_points"] = np.array(pts)
         for p in pts:
@@ -255,7 +294,7 @@ def main():
             out["pars_json"] = np.array(f.read())
     rng = np.random.Generator(np.random.PCG64(7))
     positions = rng.uniform(-1.0, 1.5, size=(64, 2))
-    cc, ca, roots, isimg = ccc_and_images(REF_LIBS["nfc"], lens, positions)
+    cc, ca, roots, isimg = ccc_and_images(REF_LIBS["strict"], lens, positions)
     out.update(cc=cc, ca=ca, img_positions=positions, img_roots=roots, img_isimg=isimg)
     np.savez_compressed(os.path.join(HERE, "config1.npz"), **out)
     print("wrote config1.npz")
@@ -263,22 +302,36 @@ def main():
     # config-2 lenses, short curves (201 points over the same 4 theta_E)
     lenses, trajs, _ = workloads.config2(seed=11, n_curves=3)
     c2 = {"lenses": lenses, "trajs": trajs, "n": 200}
-    for k in range(len(lenses)):
-        c, a = run_curve(REF_LIBS["nfc"], lenses[k], trajs[k], 200)
-        c2["counts_%d" % k], c2["amps_%d" % k] = c, a
-        # the default-flag build (FMA contraction on): the reference's own
-        # build-to-build spread on these curves
-        c2["counts_fast_%d" % k], _ = run_curve(REF_LIBS["fast"], lenses[k], trajs[k], 200)
+    for build, key in (("strict", "counts_%d"), ("nfc", "counts_nfc_%d"),
+                       ("fast", "counts_fast_%d")):
+        for k, (c, a) in enumerate(curves(REF_LIBS[build], lenses, trajs, 200)):
+            c2[key % k] = c
+            if build == "strict":
+                c2["amps_%d" % k] = a
     np.savez_compressed(os.path.join(HERE, "config2_short.npz"), **c2)
     print("wrote config2_short.npz")
 
     if args.c2:
         lenses, trajs, n = workloads.config2(seed=0, n_curves=1)
-        c, a = run_curve(REF_LIBS["nfc"], lenses[0], trajs[0], n)
-        cf, _ = run_curve(REF_LIBS["fast"], lenses[0], trajs[0], n)
+        res = {b: POOL.submit(run_curve, REF_LIBS[b], lenses[0], trajs[0], n) for b in REF_LIBS}
+        (c, a), (cn, _), (cf, _) = [res[b].result() for b in ("strict", "nfc", "fast")]
         np.savez_compressed(os.path.join(HERE, "config2_seed0.npz"), lenses=lenses, trajs=trajs,
-                            n=n, counts=c, amps=a, counts_fast=cf)
+                            n=n, counts=c, amps=a, counts_nfc=cn, counts_fast=cf)
         print("wrote config2_seed0.npz")
+
+    if args.bench:
+        bench_fixture()
+
+
+def bench_fixture():
+    """The benchmark's workload: 8 config-2 curves of seed 2024 (rank 0),
+    strict build."""
+    lenses, trajs, n = workloads.config2(seed=2024, n_curves=8)
+    res = curves(REF_LIBS["strict"], lenses, trajs, n)
+    np.savez_compressed(os.path.join(HERE, "bench_seed2024.npz"), lenses=lenses, trajs=trajs,
+                        n=n, counts=np.stack([c for c, _ in res]),
+                        amps=np.stack([a for _, a in res]))
+    print("wrote bench_seed2024.npz")
 
 
 if __name__ == "__main__":

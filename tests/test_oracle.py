@@ -79,8 +79,13 @@ def test_images_match_reference(oracle_lib, golden_c1):
             assert np.min(np.abs(mine - z)) < 1e-9
 
 
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
 @pytest.mark.parametrize("tag,v", [("uniform", 0.0), ("default", -1.0), ("linear05", 0.5)])
 def test_config1_counts_match_reference(oracle_lib, golden_c1, tag, v):
+    """Config 1, all 101 points: ray counts and magnifications equal the
+    strict reference build's bit for bit (same fill order, same FP64 sums)."""
     lens, traj, n = workloads.config1()
     o = oracle_lib.OracleIRS(*lens[:5], lens[5], n, int(lens[7]))
     if v >= 0:
@@ -88,19 +93,8 @@ def test_config1_counts_match_reference(oracle_lib, golden_c1, tag, v):
     else:
         o.set_limb_darkening("default", 0.0)
     amps, counts = o.lc_irs(*traj)
-    _, _, fragile = oracle_lib.OracleIRS(*lens[:5], lens[5], n, int(lens[7])).lc_seeds(*traj)
-    ref = golden_c1["counts_%s_nfc" % tag]
-    robust = fragile == 0
-    # every point whose image decisions are not at the filter radius agrees
-    assert np.array_equal(counts[robust], ref[robust])
-    # the fragile points are few, and explained by quirk Q4/filter radius
-    assert robust.sum() >= len(counts) - 3
-    same = counts[:n] == ref[:n]
-    ramp = golden_c1["amps_%s_nfc" % tag]
-    # same DFS summation order; the reference's -Ofast build turns r^2/rho^2
-    # into a multiplication by 1/rho^2, so weights differ in the last bit
-    tol = 0.0 if tag == "uniform" else 1e-13
-    assert np.max(np.abs(amps[:n][same] - ramp[same]) / ramp[same]) <= tol
+    assert np.array_equal(counts, golden_c1["counts_%s_strict" % tag])
+    assert np.array_equal(amps[:n], golden_c1["amps_%s_strict" % tag])
 
 
 def test_config1_amoeba_sets_match_reference(oracle_lib, golden_c1):
@@ -118,44 +112,77 @@ def test_config1_amoeba_sets_match_reference(oracle_lib, golden_c1):
         assert np.array_equal(mine, golden_c1["amoeba_%d" % p])
 
 
-def test_config2_short_counts_match_reference(oracle_lib):
-    """Config-2 lenses (small planets): the oracle equals the reference on
-    every point whose image decisions are not rounding-dependent, except
-    where the reference's two builds disagree with each other."""
-    import os
-    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_short.npz"))
+def test_config2_short_matches_reference(oracle_lib):
+    """Config-2 lenses (small planets), 3 curves x 201 points: counts and
+    magnifications equal the strict reference build's on every point."""
+    z = np.load(os.path.join(GOLDEN, "config2_short.npz"))
     n = int(z["n"])
     for k in range(len(z["lenses"])):
         L = z["lenses"][k]
-        t = z["trajs"][k]
         o = oracle_lib.OracleIRS(*L[:5], L[5], n, int(L[7]))
         o.set_limb_darkening("linear", L[6])
-        seeds, cnt, fragile = o.lc_seeds(*t)
-        ref, ref_fast = z["counts_%d" % k], z["counts_fast_%d" % k]
-        # fill a spread of points (the whole curve would take ~10 s per curve)
-        for p in range(0, n + 1, 10):
-            if fragile[p] or ref[p] != ref_fast[p]:
-                continue
-            x = t[0] + (t[2] - t[0]) * (p / n)
-            y = t[1] + (t[3] - t[1]) * (p / n)
-            _, c = o.fill(x, y, seeds[p, :cnt[p]])
-            assert c == ref[p], (k, p)
+        amps, counts = o.lc_irs(*z["trajs"][k])
+        assert np.array_equal(counts, z["counts_%d" % k]), (k, np.nonzero(counts != z["counts_%d" % k]))
+        assert np.array_equal(amps[:n], z["amps_%d" % k]), k
 
 
-def test_reference_build_spread_is_small():
-    """The reference's own builds (FMA contraction off/on) differ by a few
-    rays on points with tiny images next to small-mass lenses."""
-    import os
-    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_short.npz"))
+def _sampled_counts(oracle_lib, L, t, n, points):
+    """Counts at the given points: the whole warm-start chain (every point's
+    seeds, in order), then the fill of the sampled points only."""
+    o = oracle_lib.OracleIRS(*L[:5], L[5], n, int(L[7]))
+    o.set_limb_darkening("linear", L[6])
+    seeds, cnt, _ = o.lc_seeds(*t)
+    out = []
+    for p in points:
+        x = t[0] + (t[2] - t[0]) * (p / n)
+        y = t[1] + (t[3] - t[1]) * (p / n)
+        out.append(o.fill(x, y, seeds[p, :cnt[p]])[1])
+    return np.array(out, np.uint64)
+
+
+def test_config2_seed0_matches_reference(oracle_lib):
+    """The 5000-point curve: every point's seeds through the single chain;
+    counts at every 25th point and at every point where the reference's
+    -Ofast builds disagree with its strict build equal the strict build's."""
+    z = np.load(os.path.join(GOLDEN, "config2_seed0.npz"))
+    n = int(z["n"])
+    ref = z["counts"]
+    spread = np.nonzero((z["counts_nfc"] != ref) | (z["counts_fast"] != ref))[0]
+    pts = np.union1d(np.arange(0, n + 1, 25), spread)
+    got = _sampled_counts(oracle_lib, z["lenses"][0], z["trajs"][0], n, pts)
+    assert np.array_equal(got, ref[pts]), pts[got != ref[pts]]
+
+
+def test_bench_workload_matches_reference(oracle_lib):
+    """The benchmark's 8 curves (seed 2024): counts at every 125th point of
+    each curve equal the strict reference build's."""
+    z = np.load(os.path.join(GOLDEN, "bench_seed2024.npz"))
+    n = int(z["n"])
+    pts = np.arange(0, n + 1, 125)
+    for k in range(len(z["lenses"])):
+        got = _sampled_counts(oracle_lib, z["lenses"][k], z["trajs"][k], n, pts)
+        assert np.array_equal(got, z["counts"][k][pts]), (k, pts[got != z["counts"][k][pts]])
+
+
+def test_reference_build_spread():
+    """The reference's -Ofast builds (FMA contraction off/on) re-associate its
+    coefficient expressions at the compiler's discretion: their counts leave
+    the strict build's at points where an image next to a small-mass lens
+    sits at the 1e-6 filter radius, by a few rays each."""
+    z = np.load(os.path.join(GOLDEN, "config2_short.npz"))
     for k in range(len(z["lenses"])):
         a = z["counts_%d" % k].astype(np.int64)
-        b = z["counts_fast_%d" % k].astype(np.int64)
-        assert np.max(np.abs(a - b)) <= 64
+        for key in ("counts_nfc_%d", "counts_fast_%d"):
+            b = z[key % k].astype(np.int64)
+            assert np.max(np.abs(a - b)) <= 64
+    s0 = np.load(os.path.join(GOLDEN, "config2_seed0.npz"))
+    for key in ("counts_nfc", "counts_fast"):
+        assert np.mean(s0[key] != s0["counts"]) < 0.03
 
 
 def test_point_source_curves_match_reference(oracle_lib):
     """Point-source curves (get_lc, lcbase.cc:40-52) against the reference
-    built without FMA contraction (tests/golden/point_lc.npz): the config-1
+    built as strict IEEE (tests/golden/point_lc.npz): the config-1
     lens to 1e-9; config-2 lenses, whose small-mass lenses make single image
     magnifications rounding-sensitive, to 1e-4 (the reference's own -Ofast
     build differs from that build by up to 45 % at single points)."""

@@ -37,6 +37,8 @@ def _bind(L):
     L.tlb_configure.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int]
     L.tlb_configure.restype = ctypes.c_int
+    L.tlb_set_chain.argtypes = [vp, ctypes.c_int]
+    L.tlb_set_chain.restype = ctypes.c_int
     L.tlb_point_lc.argtypes = [vp, f64]
     L.tlb_point_lc.restype = ctypes.c_long
     L.tlb_autotune.argtypes = [vp, ctypes.c_long, ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"),
@@ -71,6 +73,12 @@ class Batch:
 
     def configure(self, precision=-1, fill_ctas=0, table_log2=0, threads=0, block_h=0):
         return self.L.tlb_configure(self.obj, precision, fill_ctas, table_log2, threads, block_h)
+
+    def set_chain(self, points):
+        """Warm-start chain length: > 0 restarts every `points` points
+        (parallel, default 4); <= 0 one chain per curve (the reference's
+        order, exact).  Applies from the next set_trajectories."""
+        return self.L.tlb_set_chain(self.obj, int(points))
 
     def set_lenses(self, lenses):
         lenses = np.ascontiguousarray(lenses, np.float64)

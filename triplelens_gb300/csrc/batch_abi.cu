@@ -96,14 +96,7 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
     T.lens = lens_idx[i];
     T.point_base = base;
     const long np = (long)n[i] + 1;
-    for (long f = 0; f < np; f += tl::kChainChunk) {
-      tl::SeedJob j;
-      j.traj = i;
-      j.first = (int32_t)f;
-      j.count = (int32_t)std::min<long>(tl::kChainChunk, np - f);
-      j.pad = 0;
-      jobs.push_back(j);
-    }
+    tl::plan_jobs(&jobs, i, np, b->chain, -1);
     base += np;
   }
   if (base >= (1L << 31)) return -1;
@@ -134,7 +127,7 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
     tl::launch_seeds((const tl::SeedJob*)b->jobs.p, b->njobs, (const tl::Traj*)b->trajs.p,
                      (const tl::DevLens*)b->lenses.p, (const cx*)b->ca.p, (tl::PointIn*)b->points.p,
                      (int32_t*)b->seeds.p, (tl::PointOut*)b->out.p, (tl::TrialList*)b->trials.p,
-                     st);
+                     nullptr, st);
   if (phase & 2) {
     tl::Run R;
     R.trajs = (tl::Traj*)b->trajs.p;
@@ -192,6 +185,12 @@ long tlb_run_host(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_
 int tlb_stats(tl_batch* b, uint64_t* out4) {
   if (!b || !out4) return -1;
   for (int k = 0; k < 4; k++) out4[k] = b->stats[k];
+  return 0;
+}
+
+int tlb_set_chain(tl_batch* b, int points) {
+  if (!b) return -1;
+  b->chain = points;
   return 0;
 }
 
@@ -311,17 +310,7 @@ long tlb_point_lc(tl_batch* b, double* amp) {
   // point-source sampling uses n points per curve (t = i/(n-1)); reuse the
   // IRS layout (n+1 slots per curve) and leave the last slot unused
   std::vector<tl::SeedJob> jobs;
-  for (int t = 0; t < b->ntraj; t++) {
-    const uint32_t n = b->htraj[t].n;
-    for (uint32_t f = 0; f < n; f += tl::kChainChunk) {
-      tl::SeedJob j;
-      j.traj = t;
-      j.first = (int32_t)f;
-      j.count = (int32_t)std::min<uint32_t>(tl::kChainChunk, n - f);
-      j.pad = 0;
-      jobs.push_back(j);
-    }
-  }
+  for (int t = 0; t < b->ntraj; t++) tl::plan_jobs(&jobs, t, (long)b->htraj[t].n, b->chain, -1);
   tl::DevBuf dj;
   void* djp = dj.need(sizeof(tl::SeedJob) * jobs.size());
   double* da = (double*)b->amp.need(sizeof(double) * b->npoints);
@@ -330,7 +319,7 @@ long tlb_point_lc(tl_batch* b, double* amp) {
   E.check(cudaMemcpyAsync(djp, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   tl::launch_point_lc((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp, (int)jobs.size(),
-                      (const tl::DevLens*)b->lenses.p, da, E.stream);
+                      (const tl::DevLens*)b->lenses.p, da, nullptr, E.stream);
   E.check(cudaMemcpyAsync(amp, da, sizeof(double) * b->npoints, cudaMemcpyDeviceToHost, E.stream));
   bool ok = E.check(cudaStreamSynchronize(E.stream));
   cudaFree(djp);

@@ -18,6 +18,7 @@ struct tl_batch {
   tl::DevBuf trajs, jobs, points, seeds, out, amp, trials;
   std::vector<tl::Traj> htraj;
   int precision = 1;
+  int chain = tl::kChainChunk;   // warm-start chain length (<= 0: whole curve)
   uint64_t stats[4] = {0, 0, 0, 0};
   // captured seeds + fill of the current trajectories (tlb_graph_capture)
   cudaGraphExec_t graph = nullptr;

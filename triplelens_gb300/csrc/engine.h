@@ -14,12 +14,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "tl_math.h"
 
 namespace tl {
 
 constexpr int kMaxSeeds = 64;     // seed pixels kept per point
-constexpr int kChainChunk = 4;    // points per warm-start chain (seed kernel)
+constexpr int kChainChunk = 4;    // points per warm-start chain in the fast mode
 
 // status bits of a point (PointOut::status)
 enum : uint32_t {
@@ -40,6 +42,8 @@ struct DevLens {
   cx box_max[kBranches];
   int32_t ray_binary;      // m3 == 0: two-lens ray map (lcirs.cc:28-36)
   int32_t ppr;
+  cx heap0[5];             // sample 10 of critical-curve branches 0..4: the
+                           // warm-start chain's heap state after construction
 };
 
 struct LensSpec {          // host-side input of the lens set-up kernel
@@ -69,8 +73,14 @@ struct SeedJob {
   int32_t traj;
   int32_t first;           // first point index within the curve
   int32_t count;
-  int32_t pad;
+  int32_t chain;           // >= 0: start from and save back chains[chain];
+                           // -1: start from the lens's construction state
 };
+
+// Jobs of one curve of np points: chunk > 0 restarts the warm-start chain
+// every chunk points (parallel, fast); chunk <= 0 runs the whole curve as one
+// chain, the reference's order (exact).  chain: see SeedJob.
+void plan_jobs(std::vector<SeedJob>* jobs, int traj, long np, int chunk, int chain);
 
 struct PointIn {
   double sx, sy;
@@ -114,10 +124,11 @@ struct TrialList {
 // warm-start chain over the points and their trial points)
 void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const DevLens* d_lenses,
                   const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
-                  TrialList* d_trials, cudaStream_t st);
+                  TrialList* d_trials, RootChain* d_chains, cudaStream_t st);
 
 void launch_point_lc(const Traj* d_trajs, const SeedJob* d_jobs, int njobs,
-                     const DevLens* d_lenses, double* d_amp, cudaStream_t st);
+                     const DevLens* d_lenses, double* d_amp, RootChain* d_chains,
+                     cudaStream_t st);
 
 struct FillScratch {
   uint64_t* keys;          // [ctas << cap_log2]

@@ -1008,7 +1008,8 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
     const bool skip = (S.status & kStBadInput) != 0;
     // seeds (lcirs.cc:171-174; seed rows must satisfy 0 < ny < N, 386-391)
     if (!skip && warp == 0) {
-      const unsigned ns = out[p].nseeds;
+      // at most kMaxSeeds pixels per point exist, whatever the count says
+      const unsigned ns = min(out[p].nseeds, (unsigned)kMaxSeeds);
       for (unsigned k = lane; k < ns; k += 32) {
         const int32_t sx = seeds[((size_t)p * kMaxSeeds + k) * 2];
         const int32_t sy = seeds[((size_t)p * kMaxSeeds + k) * 2 + 1];

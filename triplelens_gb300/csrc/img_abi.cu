@@ -110,8 +110,11 @@ ImgPoint* img_new(double a, double b, double th, double m2, double m3, double po
   o->s.L.z2 = tl::mk(a, 0.0);
   o->s.L.z3 = tl::mk(b * cos(th), b * sin(th));
   o->s.L.is_binary_img = (a == 0.0 || b == 0.0 || m3 == 0.0) ? 1 : 0;
+  tl::lens_finish(&o->s.L);
   o->s.pos = tl::mk(posX, posY);
-  tl::chain_reset(&o->s.ch);
+  // a lone ImgPoint starts with no cached 256-byte chunks: its warm starts
+  // read a zeroed slot past the roots
+  tl::chain_reset(&o->s.ch, nullptr);
   o->s.roots_available = 0;
   o->s.n_img = 0;
   o->s.wrong_after_check = 0;

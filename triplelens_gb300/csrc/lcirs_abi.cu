@@ -31,6 +31,9 @@ struct LightCurveIRS::Impl {
   tl::DevLens* d_lens = nullptr;
   cx* d_cc = nullptr;
   cx* d_ca = nullptr;
+  // the image solver's warm-start state, carried from call to call as the
+  // reference's ImgPoint member carries it (imgpoint.h:104-110)
+  tl::RootChain* d_chain = nullptr;
   std::vector<double> lcFull;  // n+1 magnifications
 };
 
@@ -47,6 +50,7 @@ void setup_object(LightCurveIRS* o) {
     E.check(cudaMalloc(&I->d_lens, sizeof(tl::DevLens)));
     E.check(cudaMalloc(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen));
     E.check(cudaMalloc(&I->d_ca, sizeof(cx) * tl::kBranches * tl::kCCLen));
+    E.check(cudaMalloc(&I->d_chain, sizeof(tl::RootChain)));
   }
   tl::LensSpec* d_spec = (tl::LensSpec*)E.scratch_specs.need(sizeof(tl::LensSpec));
   E.check(cudaMemcpyAsync(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, E.stream));
@@ -54,6 +58,10 @@ void setup_object(LightCurveIRS* o) {
   E.check(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost,
                           E.stream));
   E.check(cudaStreamSynchronize(E.stream));
+  // a fresh object's solver: no roots yet, the constructor's heap state
+  tl::RootChain ch;
+  tl::chain_reset(&ch, I->lens.heap0);
+  E.check(cudaMemcpy(I->d_chain, &ch, sizeof(ch), cudaMemcpyHostToDevice));
   E.trace("setup_object: done");
   const tl::Grid& g2 = I->lens.g;
   o->grid[0] = g2.corner_x;
@@ -88,6 +96,7 @@ LightCurveIRS::~LightCurveIRS() {
     cudaFree(impl->d_lens);
     cudaFree(impl->d_cc);
     cudaFree(impl->d_ca);
+    cudaFree(impl->d_chain);
     delete impl;
   }
 }
@@ -171,21 +180,14 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   T.lens = 0;
   T.point_base = 0;
   std::vector<tl::SeedJob> jobs;
-  for (uint32_t f = 0; f < np; f += tl::kChainChunk) {
-    tl::SeedJob j;
-    j.traj = 0;
-    j.first = (int32_t)f;
-    j.count = (int32_t)std::min<size_t>(tl::kChainChunk, np - f);
-    j.pad = 0;
-    jobs.push_back(j);
-  }
+  tl::plan_jobs(&jobs, 0, (long)np, chainPoints, 0);
   E.trace("runFill: prepare");
   tl::Run R = E.prepare(np, 1, jobs.size(), amoebaPrintOut_);
   E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
   E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, impl->d_lens, impl->d_ca, R.points, R.seeds,
-                   R.out, R.trials, E.stream);
+                   R.out, R.trials, impl->d_chain, E.stream);
   if (extSeeds) {
     // replace the seeds with the caller's, keep the positions
     std::vector<tl::PointOut> hout(np);
@@ -193,7 +195,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
                             E.stream));
     E.check(cudaStreamSynchronize(E.stream));
     for (size_t i = 0; i < np; i++) {
-      hout[i].nseeds = (uint32_t)std::min(extN[i], tl::kMaxSeeds);
+      hout[i].nseeds = (uint32_t)std::max(0, std::min(extN[i], tl::kMaxSeeds));
       hout[i].status = 0;
     }
     E.check(cudaMemcpyAsync(R.out, hout.data(), sizeof(tl::PointOut) * np, cudaMemcpyHostToDevice,
@@ -324,20 +326,14 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   T.lens = 0;
   T.point_base = 0;
   std::vector<tl::SeedJob> jobs;
-  for (uint32_t f = 0; f < n; f += tl::kChainChunk) {
-    tl::SeedJob j;
-    j.traj = 0;
-    j.first = (int32_t)f;
-    j.count = (int32_t)std::min<uint32_t>(tl::kChainChunk, n - f);
-    j.pad = 0;
-    jobs.push_back(j);
-  }
+  tl::plan_jobs(&jobs, 0, (long)n, chainPoints, 0);
   tl::Run R = E.prepare(n, 1, jobs.size(), false);
   E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
   E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   double* d_amp = (double*)E.scratch_amp.need(sizeof(double) * n);
-  tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, E.stream);
+  tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, impl->d_chain,
+                      E.stream);
   E.check(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
                           E.stream));
   E.check(cudaStreamSynchronize(E.stream));
@@ -422,6 +418,8 @@ void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3) {
 }
 
 void lcirs_set_precision(LightCurveIRS* lc, int mode) { lc->precision = mode; }
+
+void lcirs_set_chain(LightCurveIRS* lc, int points) { lc->chainPoints = points; }
 
 void lcirs_copy_diag(LightCurveIRS* lc, uint32_t* out) {
   for (size_t i = 0; i < lc->diag.size(); i++) out[i] = lc->diag[i];

@@ -20,6 +20,8 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
+
 #include "engine.h"
 
 namespace tl {
@@ -94,6 +96,7 @@ lens_setup_kernel(const LensSpec* specs, int nlens, DevLens* lenses, cx* cc_out,
   L.z2 = mk(sp.z2x, 0.0);
   L.z3 = mk(sp.z3x, sp.z3y);
   L.is_binary_img = sp.is_binary_img;
+  lens_finish(&L);
   cx* cc = cc_out + (size_t)li * kBranches * kCCLen;
   cx* ca = ca_out + (size_t)li * kBranches * kCCLen;
 
@@ -170,6 +173,7 @@ lens_setup_kernel(const LensSpec* specs, int nlens, DevLens* lenses, cx* cc_out,
   D.ld_b = sp.ld_b;
   D.ray_binary = (sp.m3 == 0.0) ? 1 : 0;
   D.ppr = ppr;
+  for (int k = 0; k < 5; k++) D.heap0[k] = cc[k * kCCLen + 10];
   lenses[li] = D;
 }
 
@@ -270,7 +274,8 @@ caustic_scan_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const Dev
 // independent across chunks, so 32 chunks share a warp's FP64 instructions.
 __global__ void __launch_bounds__(kSeedThreads)
 seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* lenses,
-             PointIn* points, int32_t* seeds_all, PointOut* out, const TrialList* trials) {
+             PointIn* points, int32_t* seeds_all, PointOut* out, const TrialList* trials,
+             RootChain* chains) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x;
   if (ji >= njobs) return;
   const SeedJob job = jobs[ji];
@@ -279,8 +284,13 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
   const Lens L = D.L;
   const Grid g = D.g;
 
+  // a chain starts from a saved state, or from the one the reference's
+  // constructor leaves
   RootChain ch;
-  chain_reset(&ch);
+  if (job.chain >= 0)
+    ch = chains[job.chain];
+  else
+    chain_reset(&ch, D.heap0);
   cx imgs[10];
   for (int q = 0; q < job.count; q++) {
     const uint32_t i = (uint32_t)(job.first + q);
@@ -298,6 +308,8 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
       int n = chain_images(L, &ch, pos, imgs, &c_trig);
       if (wrong_count(L, n)) status |= kStImageCount;
       emit_seeds(g, imgs, n, seeds, &nseed, &status);
+      SeedList sl;
+      seed_list_start(&sl, n);
       // predicted fill size, for the fill's largest-first order: the
       // point-source magnification tracks the finite-source one closely
       // (rays ~ A pi ppr^2), plus the boundary blocks
@@ -312,8 +324,10 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
       if (tl.n > (uint32_t)kMaxTrials) status |= kStSeedOverflow;
       for (uint32_t t = 0; t < ntr; t++) {
         const int nt = chain_images(L, &ch, tl.t[t], imgs, &c_trig);
+        for (int k = 0; k < nt; k++) seed_list_push(&ch, &sl, imgs[k]);
         emit_seeds(g, imgs, nt, seeds, &nseed, &status);
       }
+      seed_list_end(&ch, &sl);
     }
     points[p] = pi;
     PointOut o;
@@ -327,31 +341,35 @@ seeds_kernel(const SeedJob* jobs, int njobs, const Traj* trajs, const DevLens* l
     o.rays_fp64 = 0;
     out[p] = o;
   }
+  if (job.chain >= 0) chains[job.chain] = ch;
 }
 
 void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const DevLens* d_lenses,
                   const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
-                  TrialList* d_trials, cudaStream_t st) {
+                  TrialList* d_trials, RootChain* d_chains, cudaStream_t st) {
   if (njobs <= 0) return;
   caustic_scan_kernel<<<(njobs + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, st>>>(
       d_jobs, njobs, d_trajs, d_lenses, d_ca, d_trials);
   const int blocks = (njobs + kSeedThreads - 1) / kSeedThreads;
   seeds_kernel<<<blocks, kSeedThreads, 0, st>>>(d_jobs, njobs, d_trajs, d_lenses, d_points, d_seeds,
-                                                d_out, d_trials);
+                                                d_out, d_trials, d_chains);
 }
 
 // ---------------------------------------------------------------------------
 // point-source light curve (lcbase.cc:40-52): t = i/(n-1), i = 0..n-1
 // ---------------------------------------------------------------------------
 __global__ void point_lc_kernel(const Traj* trajs, const SeedJob* jobs, int njobs,
-                                const DevLens* lenses, double* amp) {
+                                const DevLens* lenses, double* amp, RootChain* chains) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x;
   if (ji >= njobs) return;
   const SeedJob job = jobs[ji];
   const Traj T = trajs[job.traj];
   const Lens L = lenses[T.lens].L;
   RootChain ch;
-  chain_reset(&ch);
+  if (job.chain >= 0)
+    ch = chains[job.chain];
+  else
+    chain_reset(&ch, lenses[T.lens].heap0);
   cx imgs[10];
   const cx s = mk(T.x0, T.y0), e = mk(T.x1, T.y1);
   for (int q = 0; q < job.count; q++) {
@@ -363,12 +381,26 @@ __global__ void point_lc_kernel(const Traj* trajs, const SeedJob* jobs, int njob
     for (int k = 0; k < n; k++) a += image_amp(L, imgs[k]);
     amp[T.point_base + i] = a;
   }
+  if (job.chain >= 0) chains[job.chain] = ch;
 }
 
 void launch_point_lc(const Traj* d_trajs, const SeedJob* d_jobs, int njobs, const DevLens* d_lenses,
-                     double* d_amp, cudaStream_t st) {
+                     double* d_amp, RootChain* d_chains, cudaStream_t st) {
   if (njobs <= 0) return;
-  point_lc_kernel<<<(njobs + 63) / 64, 64, 0, st>>>(d_trajs, d_jobs, njobs, d_lenses, d_amp);
+  point_lc_kernel<<<(njobs + 63) / 64, 64, 0, st>>>(d_trajs, d_jobs, njobs, d_lenses, d_amp,
+                                                   d_chains);
+}
+
+void plan_jobs(std::vector<SeedJob>* jobs, int traj, long np, int chunk, int chain) {
+  const long step = chunk > 0 ? chunk : (np > 0 ? np : 1);
+  for (long f = 0; f < np; f += step) {
+    SeedJob j;
+    j.traj = traj;
+    j.first = (int32_t)f;
+    j.count = (int32_t)std::min<long>(step, np - f);
+    j.chain = chunk > 0 ? -1 : chain;
+    jobs->push_back(j);
+  }
 }
 
 }  // namespace tl

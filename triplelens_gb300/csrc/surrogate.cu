@@ -84,7 +84,7 @@ features_kernel(int n, const double* xy, const int32_t* lens_idx, const DevLens*
   const cx src = mk(xy[2 * (size_t)p], xy[2 * (size_t)p + 1]);
   // point-source images, cold start (imgpoint.cc:208-274)
   RootChain ch;
-  chain_reset(&ch);
+  chain_reset(&ch, nullptr);
   cx imgs[10];
   const int ni = chain_images(L, &ch, src, imgs, &s_trig);
   // A_point over the images on the IRS image plane (the IRS sees no others);

@@ -44,21 +44,111 @@ TL_HD cx neg(cx a) { return mk(-a.re, -a.im); }
 TL_HD cx conj(cx a) { return mk(a.re, -a.im); }
 TL_HD cx mul(cx a, cx b) { return mk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
 TL_HD cx scale(cx a, double s) { return mk(a.re * s, a.im * s); }
-// naive complex division (the reference's -Ofast build uses the same form)
+
+// Complex division as std::complex<double> divides in a strict IEEE build:
+// Smith's algorithm (R. L. Smith, "Algorithm 116: Complex division",
+// CACM 5(8), 1962), the method of libgcc's __divdc3.  For operands of this
+// path no scaling branch of that routine is ever taken, and scaling by a
+// power of two would not change the quotient anyway; the branch for a
+// subnormal ratio is kept.
 TL_HD cx div(cx a, cx b) {
-  double d = b.re * b.re + b.im * b.im;
-  return mk((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+  if (fabs(b.re) < fabs(b.im)) {
+    const double r = b.re / b.im, den = b.re * r + b.im;
+    if (fabs(r) > 2.2250738585072014e-308)
+      return mk((a.re * r + a.im) / den, (a.im * r - a.re) / den);
+    return mk((b.re * (a.re / b.im) + a.im) / den, (b.re * (a.im / b.im) - a.re) / den);
+  }
+  const double r = b.im / b.re, den = b.im * r + b.re;
+  if (fabs(r) > 2.2250738585072014e-308)
+    return mk((a.im * r + a.re) / den, (a.im - a.re * r) / den);
+  return mk((a.re + b.im * (a.im / b.re)) / den, (a.im - b.im * (a.re / b.re)) / den);
 }
 TL_HD cx rdiv(double x, cx b) { return div(mk(x, 0.0), b); }
 TL_HD double norm(cx a) { return a.re * a.re + a.im * a.im; }
-TL_HD double cabs(cx a) { return sqrt(a.re * a.re + a.im * a.im); }
-// principal square root, half-angle form: t = sqrt((|x| + |z|)/2)
-TL_HD cx csqrt(cx a) {
-  if (a.re == 0.0 && a.im == 0.0) return mk(0.0, a.im);
-  double t = sqrt((fabs(a.re) + cabs(a)) * 0.5);
-  if (a.re >= 0.0) return mk(t, a.im / (2.0 * t));
-  return mk(fabs(a.im) / (2.0 * t), a.im < 0.0 ? -t : t);
+
+// |z| as std::abs(complex<double>) computes it in a strict IEEE build: the
+// C library's hypot.  Method of C. F. Borges, "An improved algorithm for
+// hypot(a,b)" (2019, arXiv:1904.09481): the naive root h = sqrt(x^2 + y^2),
+// corrected by the residual h^2 - x^2 - y^2 re-expressed exactly through
+// delta = h - max or h - min (the form without fused multiply-add), with
+// power-of-two scaling far from 1.  Agrees bit for bit with glibc's hypot on
+// x86-64 (checked on 2e7 random operands).
+TL_HD double hypot_kernel(double ax, double ay) {
+  double h = sqrt(ax * ax + ay * ay), t1, t2;
+  if (h <= 2.0 * ay) {
+    const double d = h - ay;
+    t1 = ax * (2.0 * d - ax);
+    t2 = (d - 2.0 * (ax - ay)) * d;
+  } else {
+    const double d = h - ax;
+    t1 = 2.0 * d * (ax - 2.0 * ay);
+    t2 = (4.0 * d - ay) * ay + d * d;
+  }
+  return h - (t1 + t2) / (2.0 * h);
 }
+TL_HD double hypot_ieee(double x, double y) {
+  x = fabs(x);
+  y = fabs(y);
+  const double ax = x < y ? y : x, ay = x < y ? x : y;
+  const double big = 6.703903964971299e+153;    // 2^511
+  const double small = 1.4916681462400413e-154;  // 2^-511
+  const double sc = 2.409919865102884e-181;      // 2^-600
+  const double eps = 5.551115123125783e-17;      // 2^-54
+  if (ax > big) {
+    if (ay <= ax * eps) return ax + ay;
+    return hypot_kernel(ax * sc, ay * sc) / sc;
+  }
+  if (ay < small) {
+    if (ax >= ay / eps) return ax + ay;
+    return hypot_kernel(ax / sc, ay / sc) * sc;
+  }
+  if (ay <= ax * eps) return ax + ay;
+  return hypot_kernel(ax, ay);
+}
+TL_HD double cabs(cx a) { return hypot_ieee(a.re, a.im); }
+
+// Principal square root as std::sqrt(complex<double>) computes it (the C
+// library's csqrt): the half-angle form on hypot (W. Kahan, "Branch cuts for
+// complex elementary functions", 1987), with 2 Re(r) Im(r) = Im(z) giving the
+// smaller component without cancellation.
+TL_HD cx csqrt(cx a) {
+  if (a.im == 0.0) {
+    if (a.re < 0.0) return mk(0.0, copysign(sqrt(-a.re), a.im));
+    return mk(fabs(sqrt(a.re)), copysign(0.0, a.im));
+  }
+  if (a.re == 0.0) {
+    const double r = sqrt(0.5 * fabs(a.im));
+    return mk(r, copysign(r, a.im));
+  }
+  const double d = hypot_ieee(a.re, a.im);
+  if (a.re > 0.0) {
+    const double r = sqrt(0.5 * (d + a.re));
+    return mk(r, 0.5 * (a.im / r));
+  }
+  const double s = sqrt(0.5 * (d - a.re));
+  return mk(fabs(0.5 * (a.im / s)), copysign(s, a.im));
+}
+
+// Operators with std::complex<double>'s rounding: a real operand scales or
+// shifts componentwise, complex products are (ac - bd, ad + bc).
+TL_HD cx C(cx z) { return z; }
+TL_HD cx C(double d) { return mk(d, 0.0); }
+TL_HD cx operator+(cx a, cx b) { return add(a, b); }
+TL_HD cx operator+(cx a, double d) { return mk(a.re + d, a.im); }
+TL_HD cx operator+(double d, cx a) { return mk(d + a.re, a.im); }
+TL_HD cx operator-(cx a, cx b) { return sub(a, b); }
+TL_HD cx operator-(cx a, double d) { return mk(a.re - d, a.im); }
+TL_HD cx operator-(double d, cx a) { return mk(d - a.re, -a.im); }
+TL_HD cx operator-(cx a) { return neg(a); }
+TL_HD cx operator*(cx a, cx b) { return mul(a, b); }
+TL_HD cx operator*(cx a, double d) { return mk(a.re * d, a.im * d); }
+TL_HD cx operator*(double d, cx a) { return mk(d * a.re, d * a.im); }
+
+}  // namespace tl
+
+#include "tl_coeffs.h"
+
+namespace tl {
 
 // ---------------------------------------------------------------------------
 // Laguerre (laguerre.h:37-38: MAX_IT 300, MT 8)
@@ -105,11 +195,12 @@ TL_HD bool laguerre(const cx* poly, int m, cx* px, const TrigTable* trig) {
     cx b = poly[m];
     double err = cabs(b);
     cx s = mk(0.0, 0.0), f = mk(0.0, 0.0);
+    const double ax = cabs(x);  // the reference takes |x| per term: same value
     for (int j = m - 1; j >= 0; j--) {
       s = add(mul(x, s), f);
       f = add(mul(x, f), b);
       b = add(mul(x, b), poly[j]);
-      err = cabs(b) + cabs(x) * err;
+      err = cabs(b) + ax * err;
     }
     err *= kEps;
     if (cabs(b) <= err) {
@@ -181,58 +272,19 @@ struct Lens {
   double m1, m2, m3;
   cx z1, z2, z3;
   int is_binary_img;  // imgpoint.cc:64: a == 0 || b == 0 || m3 == 0
+  cx coef0[11];       // source-free polynomial part (imgpointcoeff.cc:223-278)
 };
 
-// Degree-10 lens polynomial, coefficients low -> high.  Own derivation: with
-// Q = prod(z - z_k), P = sum_i m_i prod_{k!=i}(z - z_k) and
-// R_i = (conj(zeta) - conj(z_i)) Q + P, the lens equation
-// zeta = z - sum m_i / conj(z - z_i) becomes
-//   (z - zeta) R1 R2 R3 - Q (m1 R2 R3 + m2 R1 R3 + m3 R1 R2) = 0,
-// which is the reference's polynomial (imgpointcoeff.cc:223-447) up to a
-// constant factor.
-TL_HD void pmul(const cx* a, int da, const cx* b, int db, cx* out) {
-  for (int i = 0; i <= da + db; i++) out[i] = mk(0.0, 0.0);
-  for (int i = 0; i <= da; i++)
-    for (int j = 0; j <= db; j++) out[i + j] = add(out[i + j], mul(a[i], b[j]));
-}
+// Lens from the reference's constructor arguments, after z3 = b (cos, sin)
+// has been formed with the host's libm (lens.cc:4-18, 35-40).
+TL_HD void lens_finish(Lens* L) { coeffs_nozeta(L->m2, L->m3, L->z2, L->z3, L->coef0); }
 
+// Degree-10 lens polynomial, coefficients low -> high (imgpoint.cc:164-176):
+// the cached source-free part plus the source part, term by term.
 TL_HD void lens_poly(const Lens& L, cx zeta, cx* c) {
-  const cx zs[3] = {L.z1, L.z2, L.z3};
-  const double ms[3] = {L.m1, L.m2, L.m3};
-  cx l[3][2];
-  for (int k = 0; k < 3; k++) {
-    l[k][0] = neg(zs[k]);
-    l[k][1] = mk(1.0, 0.0);
-  }
-  cx q2[3], Q[4];
-  pmul(l[0], 1, l[1], 1, q2);
-  pmul(q2, 2, l[2], 1, Q);
-  cx P[3] = {mk(0.0, 0.0), mk(0.0, 0.0), mk(0.0, 0.0)};
-  for (int i = 0; i < 3; i++) {
-    cx t[3];
-    pmul(l[(i + 1) % 3], 1, l[(i + 2) % 3], 1, t);
-    for (int d = 0; d < 3; d++) P[d] = add(P[d], scale(t[d], ms[i]));
-  }
-  cx R[3][4];
-  cx zc = conj(zeta);
-  for (int i = 0; i < 3; i++) {
-    cx f = sub(zc, conj(zs[i]));
-    for (int d = 0; d < 4; d++) R[i][d] = mul(f, Q[d]);
-    for (int d = 0; d < 3; d++) R[i][d] = add(R[i][d], P[d]);
-  }
-  cx r12[7], r13[7], r23[7], r123[10];
-  pmul(R[0], 3, R[1], 3, r12);
-  pmul(R[0], 3, R[2], 3, r13);
-  pmul(R[1], 3, R[2], 3, r23);
-  pmul(r12, 6, R[2], 3, r123);
-  cx zl[2] = {neg(zeta), mk(1.0, 0.0)};
-  pmul(zl, 1, r123, 9, c);
-  cx s[7];
-  for (int d = 0; d < 7; d++)
-    s[d] = add(add(scale(r23[d], ms[0]), scale(r13[d], ms[1])), scale(r12[d], ms[2]));
-  cx rhs[10];
-  pmul(Q, 3, s, 6, rhs);
-  for (int d = 0; d < 10; d++) c[d] = sub(c[d], rhs[d]);
+  cx d[11];
+  coeffs_zeta(L.m2, L.m3, L.z2, L.z3, zeta, d);
+  for (int k = 0; k < 11; k++) c[k] = add(L.coef0[k], d[k]);
 }
 
 // imgpoint.cc:72-90: |zeta(img) - zeta_s| < radius
@@ -243,16 +295,64 @@ TL_HD bool img_check(const Lens& L, cx img, cx src, double radius) {
   return cabs(sub(t, src)) < radius;
 }
 
-// Warm-start state of the image solver along a trajectory
-// (imgpoint.h:104-110: _tempRoots and its availability).
+// ---------------------------------------------------------------------------
+// Warm-start state of the image solver along a trajectory (imgpoint.h:104-110:
+// _tempRoots), including the heap memory the reference's warm start reads.
+//
+// ImgPoint::getRootsPrecalculated warm-starts Laguerre::solveRoots from
+// _tempRoots, whose root j = 10..1 starts from initRoots[j] (laguerre.cc:
+// 111-128): root 10 reads one element past the end of the 10-element vector.
+// That vector's buffer has capacity 16 (push_back growth), 256 bytes, and the
+// slot holds whatever its chunk held before.  glibc serves 256-byte requests
+// from a per-thread LIFO cache of freed chunks, and on this path only vectors
+// of capacity 16 use that size class: each solver's result vector, the
+// ImgPoint image list once it holds 9 images, a point's seed list while it
+// holds 9-16 seeds, and, during construction, the six critical-curve branch
+// vectors, which free their capacity-16 buffers at sample 16 (ccc.cc:88-95) -
+// five of them stay cached (the sixth goes to the caustics and the caustic
+// boxes).  The model keeps the slot-10 contents of the cached chunks (top
+// last) and of the chunk _tempRoots holds, and replays every allocation and
+// release of that size class in the reference's order.
+// ---------------------------------------------------------------------------
+constexpr int kHeapSlots = 8;   // the path never caches more than 5
+
 struct RootChain {
-  cx roots[11];  // [10] is the slot the reference reads past its 10 roots
-  int have;
+  cx roots[11];        // _tempRoots; [10] is the slot a warm start reads
+  int have;            // _tempRoots holds 10 roots
+  int heap_n;          // cached chunks
+  cx heap[kHeapSlots];
+  int temp_chunk;      // _tempRoots owns a 256-byte chunk
+  int imgs_big;        // the image list owns one (capacity 16)
 };
 
-TL_HD void chain_reset(RootChain* ch) {
+// The state right after the LightCurveIRS constructor: heap0[k] = sample 10
+// of critical-curve branch k, k = 0..4 (nullptr: an empty cache).
+TL_HD void chain_reset(RootChain* ch, const cx* heap0) {
   ch->have = 0;
   for (int k = 0; k < 11; k++) ch->roots[k] = mk(0.0, 0.0);
+  ch->heap_n = 0;
+  for (int k = 0; k < kHeapSlots; k++) ch->heap[k] = mk(0.0, 0.0);
+  if (heap0)
+    for (int k = 0; k < 5; k++) ch->heap[ch->heap_n++] = heap0[k];
+  ch->temp_chunk = 0;
+  ch->imgs_big = 0;
+}
+
+TL_HD cx heap_take(RootChain* ch) {
+  if (ch->heap_n > 0) return ch->heap[--ch->heap_n];
+  return mk(0.0, 0.0);  // a chunk carved from fresh (zeroed) memory
+}
+TL_HD void heap_give(RootChain* ch, cx slot) {
+  if (ch->heap_n < kHeapSlots) ch->heap[ch->heap_n++] = slot;
+}
+
+// _tempRoots = <solver result>: the result vector took a chunk, then the old
+// buffer was released.
+TL_HD void chain_replace_roots(RootChain* ch) {
+  const cx v = heap_take(ch);
+  if (ch->temp_chunk) heap_give(ch, ch->roots[10]);
+  ch->roots[10] = v;
+  ch->temp_chunk = 1;
 }
 
 // imgpoint.cc:160-205 (getRootsPrecalculated)
@@ -261,19 +361,30 @@ TL_HD void chain_roots(const Lens& L, RootChain* ch, cx zeta, bool force, const 
   lens_poly(L, zeta, c);
   if (!ch->have || force) {
     solve_roots(c, 10, nullptr, ch->roots, trig);
+    chain_replace_roots(ch);
     ch->have = 1;
   } else {
     cx fresh[10];
     solve_roots(c, 10, ch->roots, fresh, trig);
     for (int k = 0; k < 10; k++) ch->roots[k] = fresh[k];
-    if (!check_roots(c, 10, ch->roots)) solve_roots(c, 10, nullptr, ch->roots, trig);
+    chain_replace_roots(ch);
+    if (!check_roots(c, 10, ch->roots)) {
+      solve_roots(c, 10, nullptr, ch->roots, trig);
+      chain_replace_roots(ch);
+    }
   }
 }
 
-TL_HD int filter_images(const Lens& L, const cx* roots, cx zeta, cx* imgs) {
+TL_HD int filter_images(const Lens& L, RootChain* ch, cx zeta, cx* imgs) {
   int n = 0;
   for (int k = 0; k < 10; k++)
-    if (img_check(L, roots[k], zeta, 1.0e-6)) imgs[n++] = roots[k];
+    if (img_check(L, ch->roots[k], zeta, 1.0e-6)) {
+      imgs[n++] = ch->roots[k];
+      if (n == 9 && !ch->imgs_big) {  // the image list outgrows capacity 8
+        heap_take(ch);
+        ch->imgs_big = 1;
+      }
+    }
   return n;
 }
 
@@ -285,12 +396,40 @@ TL_HD bool wrong_count(const Lens& L, int n) {
 // imgpoint.cc:208-274, 281-286: images of zeta through the chain.
 TL_HD int chain_images(const Lens& L, RootChain* ch, cx zeta, cx* imgs, const TrigTable* trig) {
   chain_roots(L, ch, zeta, false, trig);
-  int n = filter_images(L, ch->roots, zeta, imgs);
+  int n = filter_images(L, ch, zeta, imgs);
   if (wrong_count(L, n)) {
     chain_roots(L, ch, zeta, true, trig);
-    n = filter_images(L, ch->roots, zeta, imgs);
+    n = filter_images(L, ch, zeta, imgs);
   }
   return n;
+}
+
+// A point's seed list (lcirs.cc:123, imgPos): a copy of the image list
+// (capacity = size) that doubles when full.  Its capacity-16 stage takes a
+// cached chunk and gives it back when it grows again or when the point ends;
+// slot 10 then holds seed 10.
+struct SeedList {
+  int size, cap;
+  cx slot;
+};
+TL_HD void seed_list_start(SeedList* l, int n) {
+  l->size = n;
+  l->cap = n;
+  l->slot = mk(0.0, 0.0);
+}
+TL_HD void seed_list_push(RootChain* ch, SeedList* l, cx z) {
+  if (l->size == l->cap) {
+    const int nc = l->cap ? 2 * l->cap : 1;
+    const cx old = l->slot;
+    if (nc == 16) l->slot = heap_take(ch);
+    if (l->cap == 16) heap_give(ch, old);
+    l->cap = nc;
+  }
+  if (l->size == 10 && l->cap == 16) l->slot = z;
+  l->size++;
+}
+TL_HD void seed_list_end(RootChain* ch, const SeedList* l) {
+  if (l->cap == 16) heap_give(ch, l->slot);
 }
 
 // lcbase.cc:17-38 per-image point magnification 1/|1 - |sum m_i/(z-z_i)^2|^2|

@@ -50,6 +50,7 @@ def load_lcirs(path=None):
                                         ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]
     L.lcirs_copy_stats.argtypes = [vp, ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
     L.lcirs_set_precision.argtypes = [vp, ctypes.c_int]
+    L.lcirs_set_chain.argtypes = [vp, ctypes.c_int]
     L.lcirs_copy_diag.argtypes = [vp, ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")]
     _libs[path] = L
     return L
@@ -100,6 +101,11 @@ class LC_irs(object):
 
     def set_precision(self, mode):
         self.lib_lc.lcirs_set_precision(self.obj, int(mode))
+
+    def set_chain(self, points):
+        """0: one warm-start chain over the object's life (the reference's,
+        exact); k > 0: restart every k points (parallel chunks)."""
+        self.lib_lc.lcirs_set_chain(self.obj, int(points))
 
     def last_status(self):
         return int(self.lib_lc.lcirs_last_status(self.obj))
