@@ -4,9 +4,9 @@ Outputs (in-tree, git-ignored):
   bin/liblcirs.so   LightCurveIRS C ABI + GPU engine
   bin/libccc.so     critical-curve / caustic C ABI (GPU set-up kernel)
 
-Translation units compile in parallel; seeds.cu is compiled with
---fmad=false so its FP64 arithmetic matches a -ffp-contract=off host build
-bit for bit.
+Translation units compile in parallel; seeds.cu and chain.cu are
+compiled with --fmad=false so their FP64 arithmetic matches a
+-ffp-contract=off host build bit for bit.
 """
 import os
 import shutil
@@ -26,6 +26,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 # (source, extra flags)
 UNITS = [
     ("seeds.cu", ["--fmad=false"]),
+    ("chain.cu", ["--fmad=false"]),
     ("fill.cu", []),
     ("engine_host.cu", []),
     ("lcirs_abi.cu", []),
@@ -38,11 +39,11 @@ UNITS = [
 ]
 
 LIBS = {
-    "liblcirs.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
+    "liblcirs.so": ["seeds.cu", "chain.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
                     "noalloc_abi.cu", "surrogate.cu"],
     "libccc.so": ["ccc_abi.cu"],
     "libimg.so": ["img_abi.cu"],
-    "liblccuda.so": ["seeds.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
+    "liblccuda.so": ["seeds.cu", "chain.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
                      "noalloc_abi.cu", "surrogate.cu", "lccuda_abi.cu"],
 }
 

@@ -33,7 +33,7 @@ void tlb_delete(tl_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (tl::DevBuf* d : {&b->specs, &b->lenses, &b->cc, &b->ca, &b->trajs, &b->jobs, &b->points,
-                        &b->seeds, &b->out, &b->amp, &b->trials})
+                        &b->seeds, &b->out, &b->amp, &b->trials, &b->scan, &b->prep})
     if (d->p) cudaFree(d->p);
   delete b;
 }
@@ -83,7 +83,7 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
   b->htraj.resize(ntraj);
-  std::vector<tl::SeedJob> jobs;
+  std::vector<tl::SeedJob> jobs, scan;
   long base = 0;
   for (int i = 0; i < ntraj; i++) {
     if (lens_idx[i] < 0 || lens_idx[i] >= b->nlens) return -1;
@@ -97,6 +97,7 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
     T.point_base = base;
     const long np = (long)n[i] + 1;
     tl::plan_jobs(&jobs, i, np, b->chain, -1);
+    if (b->chain <= 0) tl::plan_jobs(&scan, i, np, tl::kChainChunk, -1);
     base += np;
   }
   if (base >= (1L << 31)) return -1;
@@ -110,6 +111,14 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
   void* dout = b->out.need(sizeof(tl::PointOut) * base);
   void* dtr = b->trials.need(sizeof(tl::TrialList) * base);
   if (!dt || !dj || !dp || !dsd || !dout || !dtr) return -2;
+  b->nscan = (int)scan.size();
+  if (!scan.empty()) {
+    void* dsc = b->scan.need(sizeof(tl::SeedJob) * scan.size());
+    void* dpr = b->prep.need(sizeof(tl::PointPrep) * base);
+    if (!dsc || !dpr) return -2;
+    E.check(cudaMemcpyAsync(dsc, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+                            cudaMemcpyHostToDevice, E.stream));
+  }
   E.check(cudaMemcpyAsync(dt, b->htraj.data(), sizeof(tl::Traj) * ntraj, cudaMemcpyHostToDevice,
                           E.stream));
   E.check(cudaMemcpyAsync(dj, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
@@ -123,7 +132,13 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
   cudaStream_t st = pick(stream);
-  if (phase & 1)
+  if ((phase & 1) && b->nscan > 0)
+    tl::launch_seeds_exact((const tl::SeedJob*)b->scan.p, b->nscan, (const tl::SeedJob*)b->jobs.p,
+                           b->njobs, (const tl::Traj*)b->trajs.p, (const tl::DevLens*)b->lenses.p,
+                           (const cx*)b->ca.p, (tl::PointIn*)b->points.p, (int32_t*)b->seeds.p,
+                           (tl::PointOut*)b->out.p, (tl::TrialList*)b->trials.p,
+                           (tl::PointPrep*)b->prep.p, nullptr, st);
+  else if (phase & 1)
     tl::launch_seeds((const tl::SeedJob*)b->jobs.p, b->njobs, (const tl::Traj*)b->trajs.p,
                      (const tl::DevLens*)b->lenses.p, (const cx*)b->ca.p, (tl::PointIn*)b->points.p,
                      (int32_t*)b->seeds.p, (tl::PointOut*)b->out.p, (tl::TrialList*)b->trials.p,
@@ -318,8 +333,13 @@ long tlb_point_lc(tl_batch* b, double* amp) {
   E.check(cudaMemsetAsync(da, 0, sizeof(double) * b->npoints, E.stream));
   E.check(cudaMemcpyAsync(djp, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
-  tl::launch_point_lc((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp, (int)jobs.size(),
-                      (const tl::DevLens*)b->lenses.p, da, nullptr, E.stream);
+  if (b->chain <= 0)
+    tl::launch_point_lc_exact((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp,
+                              (int)jobs.size(), (const tl::DevLens*)b->lenses.p, da, nullptr,
+                              E.stream);
+  else
+    tl::launch_point_lc((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp, (int)jobs.size(),
+                        (const tl::DevLens*)b->lenses.p, da, nullptr, E.stream);
   E.check(cudaMemcpyAsync(amp, da, sizeof(double) * b->npoints, cudaMemcpyDeviceToHost, E.stream));
   bool ok = E.check(cudaStreamSynchronize(E.stream));
   cudaFree(djp);

@@ -15,7 +15,8 @@ struct tl_batch {
   int ntraj = 0;
   long npoints = 0;
   int njobs = 0;
-  tl::DevBuf trajs, jobs, points, seeds, out, amp, trials;
+  tl::DevBuf trajs, jobs, points, seeds, out, amp, trials, scan, prep;
+  int nscan = 0;                 // exact chain: point chunks of the scan/prep
   std::vector<tl::Traj> htraj;
   int precision = 1;
   int chain = tl::kChainChunk;   // warm-start chain length (<= 0: whole curve)

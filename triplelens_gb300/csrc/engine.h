@@ -126,6 +126,32 @@ void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const D
                   const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
                   TrialList* d_trials, RootChain* d_chains, cudaStream_t st);
 
+// caustic-crossing trial points of the points of the given chunks
+void launch_caustic_scan(const SeedJob* d_jobs, int njobs, const Traj* d_trajs,
+                         const DevLens* d_lenses, const cx* d_ca, TrialList* d_trials,
+                         cudaStream_t st);
+
+// history-free part of a point's solve: its polynomial and its cold-start
+// roots (the chain takes them whenever the reference solves cold)
+struct PointPrep {
+  cx coef[11];
+  cx cold[10];
+};
+
+// Seeds with one warm-start chain per curve, the reference's order
+// (chain.cu): the caustic scan and PointPrep over the point chunks of
+// scan_jobs, then one warp per chain job.
+void launch_seeds_exact(const SeedJob* d_scan_jobs, int nscan, const SeedJob* d_chain_jobs,
+                        int nchain, const Traj* d_trajs, const DevLens* d_lenses, const cx* d_ca,
+                        PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
+                        TrialList* d_trials, PointPrep* d_prep, RootChain* d_chains,
+                        cudaStream_t st);
+void upload_chain_tables(const TrigTable& t);
+// point-source curve with one warm-start chain per job (chain.cu)
+void launch_point_lc_exact(const Traj* d_trajs, const SeedJob* d_jobs, int njobs,
+                           const DevLens* d_lenses, double* d_amp, RootChain* d_chains,
+                           cudaStream_t st);
+
 void launch_point_lc(const Traj* d_trajs, const SeedJob* d_jobs, int njobs,
                      const DevLens* d_lenses, double* d_amp, RootChain* d_chains,
                      cudaStream_t st);

@@ -130,11 +130,13 @@ bool Engine::ensure_fill_scratch(int level) {
   return true;
 }
 
-Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump) {
+Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nscan) {
   last_error = 0;
   Run R;
   R.trajs = (Traj*)trajs_.need(sizeof(Traj) * ntraj);
   R.jobs = (SeedJob*)jobs_.need(sizeof(SeedJob) * njobs);
+  R.scan_jobs = nscan ? (SeedJob*)scan_.need(sizeof(SeedJob) * nscan) : nullptr;
+  R.prep = nscan ? (PointPrep*)prep_.need(sizeof(PointPrep) * np) : nullptr;
   R.points = (PointIn*)points_.need(sizeof(PointIn) * np);
   R.seeds = (int32_t*)seeds_.need(sizeof(int32_t) * 2 * kMaxSeeds * np);
   R.out = (PointOut*)out_.need(sizeof(PointOut) * np);

@@ -24,6 +24,8 @@ struct DevBuf {
 struct Run {
   Traj* trajs;
   SeedJob* jobs;
+  SeedJob* scan_jobs;      // exact chain: point chunks of the scan and the prep
+  PointPrep* prep;         // exact chain: per-point coefficients and cold roots
   PointIn* points;
   int32_t* seeds;
   PointOut* out;
@@ -45,7 +47,8 @@ class Engine {
   DevBuf scratch_specs, scratch_amp;
 
   // sizes the per-call buffers for npoints points, ntraj curves, njobs jobs
-  Run prepare(size_t npoints, size_t ntraj, size_t njobs, bool dump);
+  // (and nscan scan chunks for the exact chain)
+  Run prepare(size_t npoints, size_t ntraj, size_t njobs, bool dump, size_t nscan = 0);
   // runs the fill kernel over the points of R
   void fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
   void fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
@@ -65,7 +68,8 @@ class Engine {
  private:
   Engine();
   bool ensure_fill_scratch(int level);
-  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_, trials_;
+  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_, trials_, scan_,
+      prep_;
   int want_big_ctas_ = -1;   // -1: 64 when there are >= 256 CTAs, else a quarter
   unsigned big_units_ = 0;
   void* fill_base_[kFillLevels] = {};

@@ -179,15 +179,24 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   T.n = n;
   T.lens = 0;
   T.point_base = 0;
-  std::vector<tl::SeedJob> jobs;
+  std::vector<tl::SeedJob> jobs, scan;
   tl::plan_jobs(&jobs, 0, (long)np, chainPoints, 0);
+  if (chainPoints <= 0) tl::plan_jobs(&scan, 0, (long)np, tl::kChainChunk, -1);
   E.trace("runFill: prepare");
-  tl::Run R = E.prepare(np, 1, jobs.size(), amoebaPrintOut_);
+  tl::Run R = E.prepare(np, 1, jobs.size(), amoebaPrintOut_, scan.size());
   E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
   E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
-  tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, impl->d_lens, impl->d_ca, R.points, R.seeds,
-                   R.out, R.trials, impl->d_chain, E.stream);
+  if (chainPoints <= 0) {
+    E.check(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+                            cudaMemcpyHostToDevice, E.stream));
+    tl::launch_seeds_exact(R.scan_jobs, (int)scan.size(), R.jobs, (int)jobs.size(), R.trajs,
+                           impl->d_lens, impl->d_ca, R.points, R.seeds, R.out, R.trials, R.prep,
+                           impl->d_chain, E.stream);
+  } else {
+    tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, impl->d_lens, impl->d_ca, R.points,
+                     R.seeds, R.out, R.trials, impl->d_chain, E.stream);
+  }
   if (extSeeds) {
     // replace the seeds with the caller's, keep the positions
     std::vector<tl::PointOut> hout(np);
@@ -332,8 +341,12 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   double* d_amp = (double*)E.scratch_amp.need(sizeof(double) * n);
-  tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, impl->d_chain,
-                      E.stream);
+  if (chainPoints <= 0)
+    tl::launch_point_lc_exact(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp,
+                              impl->d_chain, E.stream);
+  else
+    tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, impl->d_chain,
+                        E.stream);
   E.check(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
                           E.stream));
   E.check(cudaStreamSynchronize(E.stream));

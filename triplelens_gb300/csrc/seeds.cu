@@ -46,6 +46,7 @@ void upload_trig_tables() {
     ps[j] = sin(phi);
   }
   cudaMemcpyToSymbol(c_trig, &t, sizeof(t));
+  upload_chain_tables(t);
   cudaMemcpyToSymbol(c_phase_cos, pc, sizeof(pc));
   cudaMemcpyToSymbol(c_phase_sin, ps, sizeof(ps));
 }
@@ -348,11 +349,18 @@ void launch_seeds(const SeedJob* d_jobs, int njobs, const Traj* d_trajs, const D
                   const cx* d_ca, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
                   TrialList* d_trials, RootChain* d_chains, cudaStream_t st) {
   if (njobs <= 0) return;
-  caustic_scan_kernel<<<(njobs + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, st>>>(
-      d_jobs, njobs, d_trajs, d_lenses, d_ca, d_trials);
+  launch_caustic_scan(d_jobs, njobs, d_trajs, d_lenses, d_ca, d_trials, st);
   const int blocks = (njobs + kSeedThreads - 1) / kSeedThreads;
   seeds_kernel<<<blocks, kSeedThreads, 0, st>>>(d_jobs, njobs, d_trajs, d_lenses, d_points, d_seeds,
                                                 d_out, d_trials, d_chains);
+}
+
+void launch_caustic_scan(const SeedJob* d_jobs, int njobs, const Traj* d_trajs,
+                         const DevLens* d_lenses, const cx* d_ca, TrialList* d_trials,
+                         cudaStream_t st) {
+  if (njobs <= 0) return;
+  caustic_scan_kernel<<<(njobs + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, st>>>(
+      d_jobs, njobs, d_trajs, d_lenses, d_ca, d_trials);
 }
 
 // ---------------------------------------------------------------------------
