@@ -5,15 +5,21 @@ from a seed, masses from ratios log-uniform in [1e-3, 1], separations
 log-uniform in [0.5, 2], trajectories of 4 theta_E with impact parameter
 uniform in [-0.5, 0.5], 5000 points each (5001 computed, the reference's
 sampling), rho = 1e-3, 500 rays per source radius, linear limb darkening
-v = 0.5.  A step = one batch of --curves light curves through the seeds
-kernel and the persistent fill kernel.  Synthetic, seeded data.
+v = 0.5.  A step = one batch of --curves light curves (default 152, one per
+SM) through the seeds kernels and the persistent fill kernel, every curve
+with one warm-start chain in the reference's order, so the ray counts are the
+reference's (the first 8 curves are checked against its counts).  Synthetic,
+seeded data.
 
 JSON keys: value = points/s with inputs resident in HBM (device-timed with
 CUDA events on the launching stream, L2 flushed between steps); e2e = the same
-metric through the reference's C ABI (lcirs_new / get_lc_irs / copy_lc, host
-buffers, copies inside the timed region); roofline = the fill kernel against
-the FP32 pipe; cpu_baseline = the oracle (C restatement of the reference's
-CPU IRS) on the host's cores over a bounded sample of the same points.
+metric through the reference's C ABI (lcirs_new / get_lc_irs / copy_lc per
+curve from host threads, host buffers, copies and lens set-up inside the
+timed region); parity = counts against the reference's; roofline = the fill
+kernel against the FP32 pipe; fast_chain = the same workload with chunked
+warm-start chains; cpu_baseline = the oracle (C restatement of the
+reference's CPU IRS, bit-identical to its strict build) on the host's cores
+over a bounded sample of the same points.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -43,7 +49,11 @@ def _cpu_worker(args):
     from oracle import oracle
     o = oracle.OracleIRS(*lens[:5], lens[5], n, int(lens[7]))
     o.set_limb_darkening("linear", lens[6])
+    # the seeds need the whole warm-start chain up to each sampled point; its
+    # time is charged to the sample in proportion to the points it covers
+    t0 = time.perf_counter()
     seeds, cnt, _ = o.lc_seeds(*traj)
+    t_seeds = (time.perf_counter() - t0) * len(idx) / (n + 1.0)
     t0 = time.perf_counter()
     rays = 0
     for p in idx:
@@ -51,19 +61,20 @@ def _cpu_worker(args):
         y = traj[1] + (traj[3] - traj[1]) * (p / n)
         _, c = o.fill(x, y, seeds[p, :cnt[p]])
         rays += c
-    return time.perf_counter() - t0, len(idx), rays
+    return time.perf_counter() - t0 + t_seeds, len(idx), rays, t_seeds
 
 
 def cpu_baseline(pool, procs, lenses, trajs, n, sample_points):
-    """Times the oracle's fill on `sample_points` points spread over the
-    curves, split over `procs` processes; returns (points/s all cores,
-    points/s one core, rays/s all cores, description)."""
+    """Times the oracle (image chain + fill) on `sample_points` points spread
+    over the curves, split over `procs` processes; returns (points/s all
+    cores, points/s one core, rays/s all cores, description, busy seconds)."""
     ncurves = len(lenses)
-    per_curve = max(1, sample_points // ncurves)
+    use = min(ncurves, max(1, sample_points))
+    per_curve = max(1, sample_points // use)
     tasks = []
-    for k in range(ncurves):
+    for k in range(use):
         pts = np.linspace(0, n, per_curve, dtype=np.int64)
-        for chunk in np.array_split(pts, max(1, procs // ncurves)):
+        for chunk in np.array_split(pts, max(1, procs // use)):
             if len(chunk):
                 tasks.append((lenses[k], trajs[k], n, chunk.tolist()))
     t0 = time.perf_counter()
@@ -72,8 +83,9 @@ def cpu_baseline(pool, procs, lenses, trajs, n, sample_points):
     busy = sum(r[0] for r in res)
     npts = sum(r[1] for r in res)
     rays = sum(r[2] for r in res)
-    desc = "%d points spread over %d curves, oracle fill from oracle seeds, %d processes" % (
-        npts, ncurves, procs)
+    t_seed = sum(r[3] for r in res)
+    desc = ("%d points spread over %d curves: oracle image chain (charged pro rata, %.2f s) + "
+            "oracle fill, %d processes" % (npts, use, t_seed, procs))
     return npts / wall, npts / busy, rays / wall, desc, busy
 
 
@@ -195,6 +207,7 @@ def config4_leg(seed, curves, reps):
     from triplelens_gb300.batch import Batch
     lenses, trajs, n = workloads.config4(seed + 3, n_curves=curves)
     b = Batch()
+    b.set_chain(0)
     b.set_lenses(lenses)
     npts = b.set_trajectories(trajs, np.arange(curves), np.full(curves, n))
     t0 = time.perf_counter()
@@ -309,17 +322,74 @@ def max_over_ranks(value, dist, device):
     return float(t.item())
 
 
+def parity_vs_fixture(cnt, n, ncurves, seed, rank):
+    """Ray counts of the benchmark's first curves against the reference's own
+    counts for them (tests/golden/bench_seed2024.npz, strict IEEE build of
+    the reference, 8 curves of seed 2024)."""
+    path = os.path.join(ROOT, "tests", "golden", "bench_seed2024.npz")
+    if rank != 0 or seed != 2024 or not os.path.exists(path):
+        return None
+    z = np.load(path)
+    if int(z["n"]) != n:
+        return None
+    k = min(ncurves, len(z["counts"]))
+    ref = z["counts"][:k].ravel()
+    got = cnt[:k * (n + 1)]
+    return {"points": int(len(ref)), "mismatches": int(np.sum(got != ref)),
+            "reference": "ray counts of the reference's own IRS (strict IEEE build), "
+                         "first %d curves" % k}
+
+
+def status_counts(st):
+    return {"table_full": int(((st & 4) != 0).sum()), "timeout": int(((st & 8) != 0).sum()),
+            "edge": int(((st & 2) != 0).sum()), "image_count": int(((st & 16) != 0).sum()),
+            "seed_overflow": int(((st & 1) != 0).sum())}
+
+
+def e2e_objects(lenses, trajs, n, chain, threads):
+    """The reference-facing C ABI (lcirs_new / set_limb_darkening /
+    get_lc_irs / copy_lc) with host buffers, one object per curve, the curves
+    driven from a pool of host threads as independent objects (their seeds
+    run concurrently; their fills take turns).  Returns (seconds, outputs)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from triplelens_gb300.lcirs import LC_irs
+    outs = np.zeros((len(lenses), n))
+
+    def one(k):
+        L = lenses[k]
+        lc = LC_irs(*L[:5], L[5], n, int(L[7]))
+        lc.set_verbose(0)
+        lc.set_chain(chain)
+        lc.set_limb_darkening("linear", L[6])
+        lc.get_lc_irs(*trajs[k])
+        lc.copy_lc(outs[k])
+        return lc
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        t0 = time.perf_counter()
+        objs = list(ex.map(one, range(len(lenses))))
+        t = time.perf_counter() - t0
+    del objs
+    return t, outs
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--curves", type=int, default=8, help="light curves per step per GPU")
+    ap.add_argument("--curves", type=int, default=152, help="light curves per step per GPU")
     ap.add_argument("--points", type=int, default=5000)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-sample", type=int, default=512, help="points timed on the CPU")
+    ap.add_argument("--chain", type=int, default=0,
+                    help="warm-start chain: 0 = one per curve (the reference's, exact), "
+                         "k > 0 = restart every k points")
+    ap.add_argument("--cpu-sample", type=int, default=256, help="points timed on the CPU")
+    ap.add_argument("--e2e-threads", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fast", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-config4", action="store_true")
     ap.add_argument("--c4-curves", type=int, default=64,
@@ -338,10 +408,12 @@ def main():
     # weak scaling: every rank its own curves
     lenses, trajs, n = workloads.config2(rank_seed(args.seed, rank), n_curves=args.curves,
                                         n_points=args.points)
+    chain_desc = ("one warm-start chain per curve (the reference's order)" if args.chain <= 0
+                  else "warm-start chain restarted every %d points" % args.chain)
     config = {"workload": "config2: %d random triple lenses x %d-point curves, rho=1e-3, "
                           "500 rays/radius, linear LD v=0.5" % (args.curves, n),
               "curves_per_gpu": args.curves, "points_per_curve": n + 1, "rho": 1e-3,
-              "rays_per_radius": 500, "ld_v": 0.5, "seed": args.seed,
+              "rays_per_radius": 500, "ld_v": 0.5, "seed": args.seed, "chain": chain_desc,
               "l2": "flushed between steps (256 MiB write)",
               "parallelism": "curves sharded over %d GPU(s)" % world}
     ncpu = os.cpu_count() or 1
@@ -352,13 +424,11 @@ def main():
         import multiprocessing as mp
         pool = mp.get_context("spawn").Pool(ncpu)
         vals = []
-        total_busy = 0.0
         for step in range(args.warmup + args.steps):
-            pts_s, pts_s1, rays_s, desc, busy = cpu_baseline(
-                pool, ncpu, lenses, trajs, n, max(ncpu, args.cpu_sample // 4))
+            pts_s, pts_s1, rays_s, desc, busy = cpu_baseline(pool, ncpu, lenses, trajs, n,
+                                                             args.cpu_sample)
             if step >= args.warmup:
                 vals.append(pts_s)
-                total_busy += busy
         pool.close()
         v = float(np.mean(vals))
         line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
@@ -369,8 +439,9 @@ def main():
                                  "sample": desc + " per step"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0},
-                "note": "the reference's own CPU IRS cannot be built on this host (its sources "
-                        "are not present); its C restatement (oracle/) is timed instead"}
+                "note": "the reference's CPU IRS compiles only for x86 (lcirs.cc uses AVX "
+                        "intrinsics) and its sources are not on this host; its C restatement "
+                        "(oracle/), which reproduces its strict IEEE build bit for bit, is timed"}
         print(json.dumps(line))
         return
 
@@ -388,9 +459,9 @@ def main():
         dist.init_process_group("nccl")
 
     from triplelens_gb300.batch import Batch
-    from triplelens_gb300.lcirs import LC_irs
 
     b = Batch()
+    b.set_chain(args.chain)
     b.set_lenses(lenses)
     npts = b.set_trajectories(trajs, np.arange(len(trajs)), np.full(len(trajs), n))
     # a dedicated stream: the library launches on it and the events are
@@ -401,15 +472,15 @@ def main():
     sptr = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def step_device():
-        b.run_device(1, sptr)
+    def step_device(bb):
+        bb.run_device(1, sptr)
         e1 = torch.cuda.Event(enable_timing=True)
         e1.record(stream)
-        b.run_device(2, sptr)
+        bb.run_device(2, sptr)
         return e1
 
     for _ in range(args.warmup):
-        step_device()
+        step_device(b)
     torch.cuda.synchronize()
     amp, cnt, st = b.download(sptr)
     stats = b.stats()
@@ -430,7 +501,7 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e2 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            e1 = step_device()
+            e1 = step_device(b)
             e2.record(stream)
             e2.synchronize()
             tot_ms += e0.elapsed_time(e2)
@@ -442,33 +513,64 @@ def main():
         dist.barrier()
     ms_step = tot_ms / args.steps
     value = npts * world / (ms_step / 1e3)
+    incomplete = int(np.sum((st & 0xC) != 0))
 
-    # e2e: the reference-facing C ABI with host buffers, curve by curve
-    e2e_steps = max(1, min(args.steps, 3))
-    lc_objs = []
-    t_e2e = 0.0
-    h2d = d2h = 0
-    quiet = quiet_stdout().__enter__()
-    for it in range(e2e_steps + 1):
-        t0 = time.perf_counter()
-        for k in range(len(lenses)):
-            L = lenses[k]
-            lc = LC_irs(*L[:5], L[5], n, int(L[7]))
-            lc.set_verbose(0)
-            lc.set_limb_darkening("linear", L[6])
-            lc.get_lc_irs(*trajs[k])
-            out = np.zeros(n)
-            lc.copy_lc(out)
-            del lc
+    # the same workload with chunked warm-start chains (parallel seeds)
+    fast = None
+    if not args.no_fast and args.chain <= 0:
+        bf = Batch()
+        bf.set_chain(4)
+        bf.set_lenses(lenses)
+        bf.set_trajectories(trajs, np.arange(len(trajs)), np.full(len(trajs), n))
+        step_device(bf)
         torch.cuda.synchronize()
-        if it > 0:  # first pass is a warm-up
-            t_e2e += time.perf_counter() - t0
-    quiet.__exit__()
-    # bytes across the host boundary per step (per curve: lens + trajectory
-    # parameters in, per-point results out)
-    h2d = len(lenses) * (8 * 8 + 4 * 8)
-    d2h = len(lenses) * (n + 1) * 48
-    e2e_value = npts * world / (t_e2e / e2e_steps)
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e2 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e1 = step_device(bf)
+        e2.record(stream)
+        e2.synchronize()
+        _, fcnt, _ = bf.download(sptr)
+        fast = {"chain": "restarted every 4 points", "ms_per_step": e0.elapsed_time(e2),
+                "seeds_ms": e0.elapsed_time(e1),
+                "points_per_s": npts / (e0.elapsed_time(e2) / 1e3),
+                "count_mismatches_vs_exact": int(np.sum(fcnt != cnt)),
+                "parity": parity_vs_fixture(fcnt, n, len(lenses), args.seed, rank)}
+        del bf
+
+    e2e = None
+    if not args.no_e2e:
+        threads = max(1, min(len(lenses), args.e2e_threads))
+        with quiet_stdout():
+            e2e_objects(lenses, trajs, n, args.chain, threads)          # warm-up pass
+            torch.cuda.synchronize()
+            t_e2e, outs = e2e_objects(lenses, trajs, n, args.chain, threads)
+        same = bool(np.array_equal(outs.ravel(),
+                                   amp.reshape(len(lenses), n + 1)[:, :n].ravel()))
+        # bytes across the host boundary per step (per curve: lens + trajectory
+        # parameters in, n magnifications out)
+        e2e = {"value": npts * world / t_e2e, "unit": UNIT,
+               "h2d_bytes_per_step": len(lenses) * (8 * 8 + 4 * 8),
+               "d2h_bytes_per_step": len(lenses) * n * 8,
+               "path": "lcirs_new/set_limb_darkening/get_lc_irs/copy_lc per curve (reference C "
+                       "ABI), %d host threads, lens set-up included" % threads,
+               "magnifications_equal_device_run": same}
+        # the batched C ABI from host buffers (tl_batch.h: one call per batch)
+        bh = Batch()
+        bh.set_chain(args.chain)
+        ampb = np.zeros(npts)
+        cntb = np.zeros(npts, np.uint64)
+        stb = np.zeros(npts, np.uint32)
+        for it in range(2):
+            t0 = time.perf_counter()
+            bh.set_lenses(lenses)
+            bh.run_host(trajs, np.arange(len(trajs)), np.full(len(trajs), n), ampb, cntb, stb)
+            t_b = time.perf_counter() - t0
+        e2e["batch_api"] = {"value": npts * world / t_b, "unit": UNIT,
+                            "path": "tlb_set_lenses + tlb_run_host (host buffers in and out)",
+                            "counts_equal_device_run": bool(np.array_equal(cntb, cnt))}
+        del bh
 
     peaks = measured_peaks()
     clocks = clk.summary(local_rank)
@@ -490,9 +592,11 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded random lenses and trajectories)", "config": config,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h,
-                "path": "lcirs_new/get_lc_irs/copy_lc per curve (reference C ABI)"},
+        "e2e": e2e,
+        "parity": parity_vs_fixture(cnt, n, len(lenses), args.seed, rank),
+        "incomplete_points": incomplete,
+        "status_counts": status_counts(st),
+        "seeds_ms_per_step": ms_step - fill_ms / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": achieved / peak_tf, "traffic": traffic,
                      "kernel": "fill_kernel (+ overflow retries)",
@@ -505,10 +609,12 @@ def main():
                  "fp64_per_step": int(stats[1]), "tiles_per_step": int(stats[2]),
                  "accepted_per_s": float(stats[3]) * world / (ms_step / 1e3),
                  "status_or": int(np.bitwise_or.reduce(st))},
+        "fast_chain": fast,
         "clocks": clocks,
-        # per step: caustic scan + seeds, 3 ordering kernels, the fill, and two
+        # per step: caustic scan, point prep and the chain kernel (or the scan
+        # and the chunked seeds kernel), 3 ordering kernels, the fill, and two
         # overflow levels (collect + fill each)
-        "gpu_launches": 10 * args.steps,
+        "gpu_launches": (11 if args.chain <= 0 else 10) * args.steps,
     }
     if rank == 0 and not args.no_config4:
         line["config4"] = config4_leg(args.seed, args.c4_curves, max(1, min(args.steps, 3)))

@@ -28,3 +28,18 @@ def test_reference_arm_prints_one_json_line():
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "points/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_parity_vs_fixture_counts_mismatches():
+    """The bench's parity check reads the reference's counts of its first
+    curves from the committed fixture and counts differing points."""
+    import numpy as np
+    import bench
+    z = np.load(os.path.join(ROOT, "tests", "golden", "bench_seed2024.npz"))
+    n = int(z["n"])
+    cnt = np.concatenate([z["counts"].ravel(), np.zeros(3 * (n + 1), np.uint64)])
+    p = bench.parity_vs_fixture(cnt, n, 11, 2024, 0)
+    assert p["points"] == 8 * (n + 1) and p["mismatches"] == 0
+    cnt[5] += 1
+    assert bench.parity_vs_fixture(cnt, n, 11, 2024, 0)["mismatches"] == 1
+    assert bench.parity_vs_fixture(cnt, n, 11, 7, 0) is None

@@ -315,7 +315,12 @@ int tlb_graph_launch(tl_batch* b, void* stream) {
   if (!b || !b->graph) return -1;
   if (b->npoints != b->graph_points || b->njobs != b->graph_jobs) return -1;
   tl::Engine& E = tl::Engine::get();
-  return E.check(cudaGraphLaunch(b->graph, pick(stream))) ? 0 : -2;
+  std::lock_guard<std::mutex> g(E.mu);
+  cudaStream_t st = pick(stream);
+  E.fill_after(st);
+  const bool ok = E.check(cudaGraphLaunch(b->graph, st));
+  E.fill_mark(st);
+  return ok ? 0 : -2;
 }
 
 long tlb_point_lc(tl_batch* b, double* amp) {

@@ -43,6 +43,7 @@ Engine::Engine() {
     abort();
   }
   check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  check(cudaEventCreateWithFlags(&fill_done_, cudaEventDisableTiming));
   upload_trig_tables();
   if (const char* c = getenv("TL_FILL_CAP_LOG2")) want_cap_log2_ = atoi(c);
   if (const char* c = getenv("TL_TRACE")) {
@@ -66,7 +67,8 @@ void Engine::trace(const char* what) {
   if (!tracing) return;
   static const auto t0 = std::chrono::steady_clock::now();
   const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  fprintf(stderr, "[tl %10.4f] %s\n", t, what);
+  fprintf(stderr, "[tl %10.4f t%zx] %s\n", t,
+          (size_t)std::hash<std::thread::id>()(std::this_thread::get_id()) & 0xfff, what);
   fflush(stderr);
 }
 
@@ -93,6 +95,7 @@ void Engine::set_fill_config(int ctas, int cap_log2, int threads, int block_h, i
                                       fs_[0].cap_log2 + (block_h_ == 32 ? 2 : (block_h_ == 16 ? 1 : 0)) !=
                                           want_cap_log2_))) {
       cudaStreamSynchronize(stream);
+      cudaEventSynchronize(fill_done_);   // a fill may run on another stream
       cudaFree(fill_base_[level]);
       fill_base_[level] = nullptr;
       fs_[level] = FillScratch{};
@@ -130,29 +133,34 @@ bool Engine::ensure_fill_scratch(int level) {
   return true;
 }
 
-Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nscan) {
-  last_error = 0;
+Run RunBufs::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nscan,
+                     cudaStream_t st) {
   Run R;
-  R.trajs = (Traj*)trajs_.need(sizeof(Traj) * ntraj);
-  R.jobs = (SeedJob*)jobs_.need(sizeof(SeedJob) * njobs);
-  R.scan_jobs = nscan ? (SeedJob*)scan_.need(sizeof(SeedJob) * nscan) : nullptr;
-  R.prep = nscan ? (PointPrep*)prep_.need(sizeof(PointPrep) * np) : nullptr;
-  R.points = (PointIn*)points_.need(sizeof(PointIn) * np);
-  R.seeds = (int32_t*)seeds_.need(sizeof(int32_t) * 2 * kMaxSeeds * np);
-  R.out = (PointOut*)out_.need(sizeof(PointOut) * np);
-  R.trials = (TrialList*)trials_.need(sizeof(TrialList) * np);
+  R.trajs = (Traj*)trajs.need(sizeof(Traj) * ntraj);
+  R.jobs = (SeedJob*)jobs.need(sizeof(SeedJob) * njobs);
+  R.scan_jobs = nscan ? (SeedJob*)scan.need(sizeof(SeedJob) * nscan) : nullptr;
+  R.prep = nscan ? (PointPrep*)prep.need(sizeof(PointPrep) * np) : nullptr;
+  R.points = (PointIn*)points.need(sizeof(PointIn) * np);
+  R.seeds = (int32_t*)seeds.need(sizeof(int32_t) * 2 * kMaxSeeds * np);
+  R.out = (PointOut*)out.need(sizeof(PointOut) * np);
+  R.trials = (TrialList*)trials.need(sizeof(TrialList) * np);
   R.dump = nullptr;
   R.dump_count = nullptr;
   R.dump_cap = 0;
   if (dump) {
     const size_t cap = 1u << 22;  // tiles
-    char* b = (char*)dump_.need(sizeof(uint32_t) * kDumpWords * cap + 16);
+    char* b = (char*)this->dump.need(sizeof(uint32_t) * kDumpWords * cap + 16);
     R.dump_count = (unsigned*)b;
     R.dump = (uint32_t*)(b + 16);
     R.dump_cap = (unsigned)cap;
-    check(cudaMemsetAsync(R.dump_count, 0, sizeof(unsigned), stream));
+    cudaMemsetAsync(R.dump_count, 0, sizeof(unsigned), st);
   }
   return R;
+}
+
+Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nscan) {
+  last_error = 0;
+  return run_.prepare(np, ntraj, njobs, dump, nscan, stream);
 }
 
 void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
@@ -161,6 +169,12 @@ void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
 
 void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
   if (!ensure_fill_scratch(0)) return;
+  // the tables are shared: start after the previous fill, on any stream (a
+  // graph being captured is ordered at its launch instead)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  check(cudaStreamIsCapturing(st, &cap));
+  const bool capturing = cap != cudaStreamCaptureStatusNone;
+  if (!capturing) fill_after(st);
   FillScratch s = fs_[0];
   // largest points first; the head of the list goes to the large tables
   char* ob = (char*)order_.need(sizeof(int32_t) * np + 1024);
@@ -242,7 +256,11 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     launch_collect_overflow(R.out, (int)np, list, count, st);
     launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, sl, mode, threads_, st, list, count);
   }
+  if (!capturing) fill_mark(st);
   check(cudaGetLastError());
 }
+
+void Engine::fill_after(cudaStream_t st) { check(cudaStreamWaitEvent(st, fill_done_, 0)); }
+void Engine::fill_mark(cudaStream_t st) { check(cudaEventRecord(fill_done_, st)); }
 
 }  // namespace tl

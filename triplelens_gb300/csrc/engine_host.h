@@ -35,6 +35,18 @@ struct Run {
   unsigned dump_cap;
 };
 
+// The per-call device buffers of a run (grow-only).  The engine keeps one
+// set; every LightCurveIRS object keeps its own, so that the seeds of
+// different objects run concurrently (only the fill shares the engine's
+// tables).
+struct RunBufs {
+  DevBuf trajs, jobs, scan, prep, points, seeds, out, trials, dump;
+  // sizes the buffers for npoints points, ntraj curves, njobs jobs (and nscan
+  // scan chunks for the exact chain); clears the dump counter on st
+  Run prepare(size_t npoints, size_t ntraj, size_t njobs, bool dump, size_t nscan,
+              cudaStream_t st);
+};
+
 // device copy of an object's lens, grid and limb darkening (lcirs_abi.cu)
 const DevLens* object_device_lens(const LightCurveIRS* lc);
 
@@ -49,9 +61,16 @@ class Engine {
   // sizes the per-call buffers for npoints points, ntraj curves, njobs jobs
   // (and nscan scan chunks for the exact chain)
   Run prepare(size_t npoints, size_t ntraj, size_t njobs, bool dump, size_t nscan = 0);
-  // runs the fill kernel over the points of R
+  // runs the fill kernel over the points of R.  Fills share the engine's
+  // tables: each fill waits (on the device) for the previous one, whatever
+  // stream either was launched on.  Call with `mu` held.
   void fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
   void fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
+  // order work that uses the fill tables outside fill_on (a graph replay):
+  // fill_after makes st wait for the last fill, fill_mark records st's work
+  // as the last fill
+  void fill_after(cudaStream_t st);
+  void fill_mark(cudaStream_t st);
   bool check(cudaError_t e);
   // TL_TRACE=1: print every host step with a timestamp to stderr
   void trace(const char* what);
@@ -68,8 +87,9 @@ class Engine {
  private:
   Engine();
   bool ensure_fill_scratch(int level);
-  DevBuf trajs_, jobs_, points_, seeds_, out_, dump_, retry_, prof_, order_, trials_, scan_,
-      prep_;
+  RunBufs run_;
+  DevBuf retry_, prof_, order_;
+  cudaEvent_t fill_done_ = nullptr;   // the last fill launched
   int want_big_ctas_ = -1;   // -1: 64 when there are >= 256 CTAs, else a quarter
   unsigned big_units_ = 0;
   void* fill_base_[kFillLevels] = {};

@@ -126,24 +126,44 @@ __device__ __forceinline__ uint32_t hash_key(uint64_t k) {
   return (uint32_t)k;
 }
 
+// m / conj(w) for real m, as complex<double>(m) / conj(w) divides in a strict
+// IEEE build: Smith's algorithm (R. L. Smith, CACM 5(8), 1962) with the
+// numerator's zero imaginary part kept in every operation
+__device__ __forceinline__ void rdiv_conj(double m, double wr, double wi, double* qr, double* qi) {
+  const double br = wr, bi = -wi;
+  if (fabs(br) < fabs(bi)) {
+    const double r = __ddiv_rn(br, bi), den = __dadd_rn(__dmul_rn(br, r), bi);
+    if (fabs(r) > 2.2250738585072014e-308) {
+      *qr = __ddiv_rn(__dadd_rn(__dmul_rn(m, r), 0.0), den);
+      *qi = __ddiv_rn(__dsub_rn(__dmul_rn(0.0, r), m), den);
+    } else {
+      *qr = __ddiv_rn(__dadd_rn(__dmul_rn(br, __ddiv_rn(m, bi)), 0.0), den);
+      *qi = __ddiv_rn(__dsub_rn(__dmul_rn(br, __ddiv_rn(0.0, bi)), m), den);
+    }
+  } else {
+    const double r = __ddiv_rn(bi, br), den = __dadd_rn(__dmul_rn(bi, r), br);
+    if (fabs(r) > 2.2250738585072014e-308) {
+      *qr = __ddiv_rn(__dadd_rn(__dmul_rn(0.0, r), m), den);
+      *qi = __ddiv_rn(__dsub_rn(0.0, __dmul_rn(m, r)), den);
+    } else {
+      *qr = __ddiv_rn(__dadd_rn(m, __dmul_rn(bi, __ddiv_rn(0.0, br))), den);
+      *qi = __ddiv_rn(__dsub_rn(0.0, __dmul_rn(bi, __ddiv_rn(m, br))), den);
+    }
+  }
+}
+
 // FP64 ray map in the reference's irsSIMD lane order (lcirs.cc:290-341):
 // lanes (z3, z2, z1, zeta_s); every operation separately rounded.
 __device__ __noinline__ double irs_exact(const Ctx& c, double x, double y) {
   if (c.binary) {
-    // irsBinary (lcirs.cc:345-353) with the naive complex division
-    cx img = mk(x, y);
-    cx w1 = mk(__dsub_rn(img.re, 0.0), __dsub_rn(img.im, 0.0));
-    double d1 = __dadd_rn(__dmul_rn(w1.re, w1.re), __dmul_rn(w1.im, w1.im));
-    // m1 / conj(w1) = (m1*w1.re + 0*(-w1.im))/d1 , (0*w1.re - m1*(-w1.im))/d1
-    double q1r = __ddiv_rn(__dadd_rn(__dmul_rn(c.m1, w1.re), __dmul_rn(0.0, -w1.im)), d1);
-    double q1i = __ddiv_rn(__dsub_rn(__dmul_rn(0.0, w1.re), __dmul_rn(c.m1, -w1.im)), d1);
-    cx w2 = mk(__dsub_rn(img.re, c.z2x), __dsub_rn(img.im, 0.0));
-    double d2 = __dadd_rn(__dmul_rn(w2.re, w2.re), __dmul_rn(w2.im, w2.im));
-    double q2r = __ddiv_rn(__dadd_rn(__dmul_rn(c.m2, w2.re), __dmul_rn(0.0, -w2.im)), d2);
-    double q2i = __ddiv_rn(__dsub_rn(__dmul_rn(0.0, w2.re), __dmul_rn(c.m2, -w2.im)), d2);
-    double tr = __dsub_rn(__dsub_rn(img.re, q1r), q2r);
-    double ti = __dsub_rn(__dsub_rn(img.im, q1i), q2i);
-    double er = __dsub_rn(tr, c.sx), ei = __dsub_rn(ti, c.sy);
+    // irsBinary (lcirs.cc:345-353): img - m1/conj(img - z1) - m2/conj(img - z2),
+    // each quotient by Smith's complex division (the strict build's __divdc3)
+    double q1r, q1i, q2r, q2i;
+    rdiv_conj(c.m1, __dsub_rn(x, 0.0), __dsub_rn(y, 0.0), &q1r, &q1i);
+    rdiv_conj(c.m2, __dsub_rn(x, c.z2x), __dsub_rn(y, 0.0), &q2r, &q2i);
+    const double tr = __dsub_rn(__dsub_rn(x, q1r), q2r);
+    const double ti = __dsub_rn(__dsub_rn(y, q1i), q2i);
+    const double er = __dsub_rn(tr, c.sx), ei = __dsub_rn(ti, c.sy);
     return __dadd_rn(__dmul_rn(er, er), __dmul_rn(ei, ei));
   }
   const double wr0 = __dsub_rn(c.z3x, x), wr1 = __dsub_rn(c.z2x, x), wr2 = __dsub_rn(0.0, x),

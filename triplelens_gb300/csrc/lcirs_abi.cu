@@ -35,33 +35,48 @@ struct LightCurveIRS::Impl {
   // reference's ImgPoint member carries it (imgpoint.h:104-110)
   tl::RootChain* d_chain = nullptr;
   std::vector<double> lcFull;  // n+1 magnifications
+  // the object's own stream and buffers: objects used from different host
+  // threads set up and seed concurrently; their fills take turns on the
+  // engine's tables
+  cudaStream_t st = nullptr;
+  tl::RunBufs bufs;
+  tl::DevBuf specbuf, ampbuf;
+  bool failed = false;
+  bool ck(cudaError_t e) {
+    if (e != cudaSuccess) {
+      fprintf(stderr, "liblcirs: CUDA error %s\n", cudaGetErrorString(e));
+      failed = true;
+      return false;
+    }
+    return true;
+  }
 };
 
 namespace {
 
 void setup_object(LightCurveIRS* o) {
   tl::Engine& E = tl::Engine::get();
-  std::lock_guard<std::mutex> g(E.mu);
   E.trace("setup_object: lens set-up");
   auto* I = o->impl;
   I->spec = tl::make_lens_spec(o->a, o->b, o->th, o->m2, o->m3, o->sourceRadius,
                                o->pointsPerRadius, o->ldA, o->ldB, o->intensityCoeff);
   if (!I->d_lens) {
-    E.check(cudaMalloc(&I->d_lens, sizeof(tl::DevLens)));
-    E.check(cudaMalloc(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen));
-    E.check(cudaMalloc(&I->d_ca, sizeof(cx) * tl::kBranches * tl::kCCLen));
-    E.check(cudaMalloc(&I->d_chain, sizeof(tl::RootChain)));
+    I->ck(cudaStreamCreateWithFlags(&I->st, cudaStreamNonBlocking));
+    I->ck(cudaMalloc(&I->d_lens, sizeof(tl::DevLens)));
+    I->ck(cudaMalloc(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen));
+    I->ck(cudaMalloc(&I->d_ca, sizeof(cx) * tl::kBranches * tl::kCCLen));
+    I->ck(cudaMalloc(&I->d_chain, sizeof(tl::RootChain)));
   }
-  tl::LensSpec* d_spec = (tl::LensSpec*)E.scratch_specs.need(sizeof(tl::LensSpec));
-  E.check(cudaMemcpyAsync(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, E.stream));
-  tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, E.stream);
-  E.check(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost,
-                          E.stream));
-  E.check(cudaStreamSynchronize(E.stream));
+  tl::LensSpec* d_spec = (tl::LensSpec*)I->specbuf.need(sizeof(tl::LensSpec));
+  I->ck(cudaMemcpyAsync(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, I->st));
+  tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, I->st);
+  I->ck(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost, I->st));
+  I->ck(cudaStreamSynchronize(I->st));
   // a fresh object's solver: no roots yet, the constructor's heap state
   tl::RootChain ch;
   tl::chain_reset(&ch, I->lens.heap0);
-  E.check(cudaMemcpy(I->d_chain, &ch, sizeof(ch), cudaMemcpyHostToDevice));
+  I->ck(cudaMemcpyAsync(I->d_chain, &ch, sizeof(ch), cudaMemcpyHostToDevice, I->st));
+  I->ck(cudaStreamSynchronize(I->st));
   E.trace("setup_object: done");
   const tl::Grid& g2 = I->lens.g;
   o->grid[0] = g2.corner_x;
@@ -97,6 +112,11 @@ LightCurveIRS::~LightCurveIRS() {
     cudaFree(impl->d_cc);
     cudaFree(impl->d_ca);
     cudaFree(impl->d_chain);
+    if (impl->st) cudaStreamDestroy(impl->st);
+    for (tl::DevBuf* d : {&impl->bufs.trajs, &impl->bufs.jobs, &impl->bufs.scan, &impl->bufs.prep,
+                          &impl->bufs.points, &impl->bufs.seeds, &impl->bufs.out,
+                          &impl->bufs.trials, &impl->bufs.dump, &impl->specbuf, &impl->ampbuf})
+      if (d->p) cudaFree(d->p);
     delete impl;
   }
 }
@@ -123,11 +143,9 @@ void LightCurveIRS::setLimbDarkening(const std::string& model, double v) {
   impl->spec.ld_a = ldA;
   impl->spec.ld_b = ldB;
   impl->spec.intensity = intensityCoeff;
-  tl::Engine& E = tl::Engine::get();
-  std::lock_guard<std::mutex> g(E.mu);
-  E.check(cudaMemcpyAsync(impl->d_lens, &impl->lens, sizeof(tl::DevLens), cudaMemcpyHostToDevice,
-                          E.stream));
-  E.check(cudaStreamSynchronize(E.stream));
+  impl->ck(cudaMemcpyAsync(impl->d_lens, &impl->lens, sizeof(tl::DevLens), cudaMemcpyHostToDevice,
+                           impl->st));
+  impl->ck(cudaStreamSynchronize(impl->st));
 }
 
 void LightCurveIRS::setAmoebaPrintOut(bool on, std::string amoebaFilename,
@@ -168,7 +186,8 @@ void LightCurveIRS::printOutLCParameters() {
 void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
                             const int32_t* extSeeds, const int32_t* extN) {
   tl::Engine& E = tl::Engine::get();
-  std::lock_guard<std::mutex> g(E.mu);
+  auto* I = impl;
+  I->failed = false;
   const uint32_t n = lcLength;
   const size_t np = (size_t)n + 1;
   tl::Traj T;
@@ -183,74 +202,78 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   tl::plan_jobs(&jobs, 0, (long)np, chainPoints, 0);
   if (chainPoints <= 0) tl::plan_jobs(&scan, 0, (long)np, tl::kChainChunk, -1);
   E.trace("runFill: prepare");
-  tl::Run R = E.prepare(np, 1, jobs.size(), amoebaPrintOut_, scan.size());
-  E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
-  E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
-                          cudaMemcpyHostToDevice, E.stream));
+  tl::Run R = I->bufs.prepare(np, 1, jobs.size(), amoebaPrintOut_, scan.size(), I->st);
+  I->ck(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
+  I->ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                          cudaMemcpyHostToDevice, I->st));
   if (chainPoints <= 0) {
-    E.check(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
-                            cudaMemcpyHostToDevice, E.stream));
+    I->ck(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+                            cudaMemcpyHostToDevice, I->st));
     tl::launch_seeds_exact(R.scan_jobs, (int)scan.size(), R.jobs, (int)jobs.size(), R.trajs,
                            impl->d_lens, impl->d_ca, R.points, R.seeds, R.out, R.trials, R.prep,
-                           impl->d_chain, E.stream);
+                           impl->d_chain, I->st);
   } else {
     tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, impl->d_lens, impl->d_ca, R.points,
-                     R.seeds, R.out, R.trials, impl->d_chain, E.stream);
+                     R.seeds, R.out, R.trials, impl->d_chain, I->st);
   }
   if (extSeeds) {
     // replace the seeds with the caller's, keep the positions
     std::vector<tl::PointOut> hout(np);
-    E.check(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
-                            E.stream));
-    E.check(cudaStreamSynchronize(E.stream));
+    I->ck(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
+                            I->st));
+    I->ck(cudaStreamSynchronize(I->st));
     for (size_t i = 0; i < np; i++) {
       hout[i].nseeds = (uint32_t)std::max(0, std::min(extN[i], tl::kMaxSeeds));
       hout[i].status = 0;
     }
-    E.check(cudaMemcpyAsync(R.out, hout.data(), sizeof(tl::PointOut) * np, cudaMemcpyHostToDevice,
-                            E.stream));
-    E.check(cudaMemcpyAsync(R.seeds, extSeeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
-                            cudaMemcpyHostToDevice, E.stream));
+    I->ck(cudaMemcpyAsync(R.out, hout.data(), sizeof(tl::PointOut) * np, cudaMemcpyHostToDevice,
+                            I->st));
+    I->ck(cudaMemcpyAsync(R.seeds, extSeeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
+                            cudaMemcpyHostToDevice, I->st));
   }
   E.trace("runFill: seeds launched");
   if (E.sync_steps) {
-    E.check(cudaStreamSynchronize(E.stream));
+    I->ck(cudaStreamSynchronize(I->st));
     E.trace("runFill: seeds done");
   }
-  E.fill(R, np, impl->d_lens, precision);
+  {
+    // the fill tables are the engine's: one launch sequence at a time
+    std::lock_guard<std::mutex> g(E.mu);
+    E.fill_on(R, np, impl->d_lens, precision, I->st);
+  }
   E.trace("runFill: fill launched");
   if (E.sync_steps) {
-    E.check(cudaStreamSynchronize(E.stream));
+    I->ck(cudaStreamSynchronize(I->st));
     E.trace("runFill: fill done");
   }
   std::vector<tl::PointOut> hout(np);
-  E.check(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
-                          E.stream));
+  I->ck(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
+                          I->st));
   seeds.resize(np * 2 * tl::kMaxSeeds);
   nseeds.resize(np);
-  E.check(cudaMemcpyAsync(seeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
-                          cudaMemcpyDeviceToHost, E.stream));
+  I->ck(cudaMemcpyAsync(seeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
+                          cudaMemcpyDeviceToHost, I->st));
   std::vector<uint32_t> dump;
   unsigned ndump = 0;
   if (amoebaPrintOut_) {
-    E.check(cudaMemcpyAsync(&ndump, R.dump_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
-                            E.stream));
+    I->ck(cudaMemcpyAsync(&ndump, R.dump_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            I->st));
   }
-  E.check(cudaStreamSynchronize(E.stream));
+  I->ck(cudaStreamSynchronize(I->st));
   if (amoebaPrintOut_) {
     if (ndump > R.dump_cap) {
       std::cout << "amoeba dump truncated: " << ndump << " tiles, capacity " << R.dump_cap << "\n";
       ndump = R.dump_cap;
     }
     dump.resize((size_t)ndump * tl::kDumpWords);
-    E.check(cudaMemcpy(dump.data(), R.dump, sizeof(uint32_t) * dump.size(),
+    I->ck(cudaMemcpy(dump.data(), R.dump, sizeof(uint32_t) * dump.size(),
                        cudaMemcpyDeviceToHost));
   }
   E.trace("runFill: results copied");
   counts.resize(np);
   status.resize(np);
   diag.resize(np);
-  lastStatus = E.last_error ? 0x100u : 0u;
+  lastStatus = I->failed ? 0x100u : 0u;
   stats[0] = stats[1] = stats[2] = 0;
   const double scale = impl->lens.g.amp_scale;
   for (size_t i = 0; i < np; i++) {
@@ -322,8 +345,7 @@ void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
 }
 
 void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
-  tl::Engine& E = tl::Engine::get();
-  std::lock_guard<std::mutex> g(E.mu);
+  auto* I = impl;
   const uint32_t n = lcLength;
   if (n == 0) return;
   tl::Traj T;
@@ -336,20 +358,20 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   T.point_base = 0;
   std::vector<tl::SeedJob> jobs;
   tl::plan_jobs(&jobs, 0, (long)n, chainPoints, 0);
-  tl::Run R = E.prepare(n, 1, jobs.size(), false);
-  E.check(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, E.stream));
-  E.check(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
-                          cudaMemcpyHostToDevice, E.stream));
-  double* d_amp = (double*)E.scratch_amp.need(sizeof(double) * n);
+  tl::Run R = I->bufs.prepare(n, 1, jobs.size(), false, 0, I->st);
+  I->ck(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
+  I->ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                          cudaMemcpyHostToDevice, I->st));
+  double* d_amp = (double*)I->ampbuf.need(sizeof(double) * n);
   if (chainPoints <= 0)
     tl::launch_point_lc_exact(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp,
-                              impl->d_chain, E.stream);
+                              impl->d_chain, I->st);
   else
     tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, impl->d_chain,
-                        E.stream);
-  E.check(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
-                          E.stream));
-  E.check(cudaStreamSynchronize(E.stream));
+                        I->st);
+  I->ck(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                          I->st));
+  I->ck(cudaStreamSynchronize(I->st));
   for (size_t i = 0; i < n; i++) impl->lcFull[i] = lcVec[i];
 }
 
