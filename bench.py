@@ -546,8 +546,8 @@ def main():
             e2e_objects(lenses, trajs, n, args.chain, threads)          # warm-up pass
             torch.cuda.synchronize()
             t_e2e, outs = e2e_objects(lenses, trajs, n, args.chain, threads)
-        same = bool(np.array_equal(outs.ravel(),
-                                   amp.reshape(len(lenses), n + 1)[:, :n].ravel()))
+        ref_amp = amp.reshape(len(lenses), n + 1)[:, :n]
+        rel = float(np.max(np.abs(outs - ref_amp) / ref_amp))
         # bytes across the host boundary per step (per curve: lens + trajectory
         # parameters in, n magnifications out)
         e2e = {"value": npts * world / t_e2e, "unit": UNIT,
@@ -555,7 +555,7 @@ def main():
                "d2h_bytes_per_step": len(lenses) * n * 8,
                "path": "lcirs_new/set_limb_darkening/get_lc_irs/copy_lc per curve (reference C "
                        "ABI), %d host threads, lens set-up included" % threads,
-               "magnifications_equal_device_run": same}
+               "max_rel_diff_vs_device_run": rel}
         # the batched C ABI from host buffers (tl_batch.h: one call per batch)
         bh = Batch()
         bh.set_chain(args.chain)

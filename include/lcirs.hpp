@@ -55,6 +55,9 @@ struct LightCurveIRS {
   // pixels ((n+1) x 64 x 2, counts in extN) replace the computed ones.
   void runFill(std::complex<double> s, std::complex<double> e, const int32_t* extSeeds,
                const int32_t* extN);
+  // getLCIRS without the amoeba dump: joins concurrent calls of other objects
+  // into one launch (same results as runFill)
+  void runBatched(std::complex<double> s, std::complex<double> e);
 
  private:
   void printOutLCParameters();

@@ -394,3 +394,30 @@ def test_lccuda_abi_routes_to_the_irs(product_lib):
     a.copy_lc(out_a)
     b.copy_lc(out_b)
     assert np.max(np.abs(out_a - out_b) / np.abs(out_b)) < 1e-12
+
+
+def test_concurrent_objects_equal_lone_calls(product_lib):
+    """get_lc_irs on several objects from several host threads (batched into
+    shared launches) leaves every object with the counts and magnifications
+    of a lone call, and with the same warm-start state for its next call."""
+    from concurrent.futures import ThreadPoolExecutor
+    lenses, trajs, _ = workloads.config2(seed=9, n_curves=6, n_points=120)
+    n = 120
+    lone = []
+    for k in range(6):
+        lc = _lc(product_lib, lenses[k], n, 1)
+        lc.get_lc_irs(*trajs[k])
+        lc.get_lc_irs(*trajs[(k + 1) % 6])
+        lone.append((lc.counts(), lc.lc_full()))
+    objs = [_lc(product_lib, lenses[k], n, 1) for k in range(6)]
+
+    def run(k):
+        objs[k].get_lc_irs(*trajs[k])
+        objs[k].get_lc_irs(*trajs[(k + 1) % 6])
+        return objs[k].counts(), objs[k].lc_full()
+
+    with ThreadPoolExecutor(max_workers=6) as ex:
+        got = list(ex.map(run, range(6)))
+    for k in range(6):
+        assert np.array_equal(got[k][0], lone[k][0]), k
+        _assert_ld_close(got[k][1], lone[k][1], LD_RTOL_SPLIT)

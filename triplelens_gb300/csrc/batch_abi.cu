@@ -164,6 +164,9 @@ int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, v
   tl::Engine& E = tl::Engine::get();
   cudaStream_t st = pick(stream);
   std::vector<tl::PointOut> h(b->npoints);
+  // wait before the pageable copy: a copy that waits for kernels holds the
+  // driver's staging path and stalls other threads' copies
+  if (!E.check(cudaStreamSynchronize(st))) return -2;
   if (!E.check(cudaMemcpyAsync(h.data(), b->out.p, sizeof(tl::PointOut) * b->npoints,
                                cudaMemcpyDeviceToHost, st)))
     return -2;
@@ -345,6 +348,7 @@ long tlb_point_lc(tl_batch* b, double* amp) {
   else
     tl::launch_point_lc((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp, (int)jobs.size(),
                         (const tl::DevLens*)b->lenses.p, da, nullptr, E.stream);
+  E.check(cudaStreamSynchronize(E.stream));
   E.check(cudaMemcpyAsync(amp, da, sizeof(double) * b->npoints, cudaMemcpyDeviceToHost, E.stream));
   bool ok = E.check(cudaStreamSynchronize(E.stream));
   cudaFree(djp);

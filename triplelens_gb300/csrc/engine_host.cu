@@ -14,21 +14,34 @@
 
 namespace tl {
 
-void* DevBuf::need(size_t bytes) {
+void* DevBuf::need(size_t bytes, cudaStream_t st) {
   if (bytes == 0) bytes = 16;
   if (bytes > n) {
-    if (p) cudaFree(p);
-    p = nullptr;
+    release(st);
     size_t want = bytes + bytes / 4;
-    if (cudaMalloc(&p, want) != cudaSuccess) {
+    const cudaError_t e = st ? cudaMallocAsync(&p, want, st) : cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
       p = nullptr;
       n = 0;
-      fprintf(stderr, "liblcirs: cudaMalloc of %zu bytes failed\n", want);
+      fprintf(stderr, "liblcirs: device allocation of %zu bytes failed\n", want);
       return nullptr;
     }
+    pooled = st != nullptr;
     n = want;
   }
   return p;
+}
+
+void DevBuf::release(cudaStream_t st) {
+  if (p) {
+    if (pooled)
+      cudaFreeAsync(p, st);
+    else
+      cudaFree(p);
+  }
+  p = nullptr;
+  n = 0;
+  pooled = false;
 }
 
 Engine& Engine::get() {
@@ -44,6 +57,16 @@ Engine::Engine() {
   }
   check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   check(cudaEventCreateWithFlags(&fill_done_, cudaEventDisableTiming));
+  // freed pool memory stays with the process (stream-ordered buffers of
+  // objects are released and taken again without a trip to the driver)
+  {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   upload_trig_tables();
   if (const char* c = getenv("TL_FILL_CAP_LOG2")) want_cap_log2_ = atoi(c);
   if (const char* c = getenv("TL_TRACE")) {
@@ -136,20 +159,20 @@ bool Engine::ensure_fill_scratch(int level) {
 Run RunBufs::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nscan,
                      cudaStream_t st) {
   Run R;
-  R.trajs = (Traj*)trajs.need(sizeof(Traj) * ntraj);
-  R.jobs = (SeedJob*)jobs.need(sizeof(SeedJob) * njobs);
-  R.scan_jobs = nscan ? (SeedJob*)scan.need(sizeof(SeedJob) * nscan) : nullptr;
-  R.prep = nscan ? (PointPrep*)prep.need(sizeof(PointPrep) * np) : nullptr;
-  R.points = (PointIn*)points.need(sizeof(PointIn) * np);
-  R.seeds = (int32_t*)seeds.need(sizeof(int32_t) * 2 * kMaxSeeds * np);
-  R.out = (PointOut*)out.need(sizeof(PointOut) * np);
-  R.trials = (TrialList*)trials.need(sizeof(TrialList) * np);
+  R.trajs = (Traj*)trajs.need(sizeof(Traj) * ntraj, st);
+  R.jobs = (SeedJob*)jobs.need(sizeof(SeedJob) * njobs, st);
+  R.scan_jobs = nscan ? (SeedJob*)scan.need(sizeof(SeedJob) * nscan, st) : nullptr;
+  R.prep = nscan ? (PointPrep*)prep.need(sizeof(PointPrep) * np, st) : nullptr;
+  R.points = (PointIn*)points.need(sizeof(PointIn) * np, st);
+  R.seeds = (int32_t*)seeds.need(sizeof(int32_t) * 2 * kMaxSeeds * np, st);
+  R.out = (PointOut*)out.need(sizeof(PointOut) * np, st);
+  R.trials = (TrialList*)trials.need(sizeof(TrialList) * np, st);
   R.dump = nullptr;
   R.dump_count = nullptr;
   R.dump_cap = 0;
   if (dump) {
     const size_t cap = 1u << 22;  // tiles
-    char* b = (char*)this->dump.need(sizeof(uint32_t) * kDumpWords * cap + 16);
+    char* b = (char*)this->dump.need(sizeof(uint32_t) * kDumpWords * cap + 16, st);
     R.dump_count = (unsigned*)b;
     R.dump = (uint32_t*)(b + 16);
     R.dump_cap = (unsigned)cap;

@@ -15,10 +15,17 @@ struct LightCurveIRS;
 
 namespace tl {
 
+// Grow-only device buffer.  With a stream, the buffer comes from the
+// device's stream-ordered pool (cudaMallocAsync / cudaFreeAsync on that
+// stream), which neither waits for the device nor returns memory to the
+// system between calls; objects created and freed while a fill runs on
+// another stream then do not stall behind it.
 struct DevBuf {
   void* p = nullptr;
   size_t n = 0;
-  void* need(size_t bytes);
+  bool pooled = false;
+  void* need(size_t bytes, cudaStream_t st = nullptr);
+  void release(cudaStream_t st = nullptr);
 };
 
 struct Run {

@@ -15,6 +15,8 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <chrono>
+#include <condition_variable>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -62,14 +64,18 @@ void setup_object(LightCurveIRS* o) {
                                o->pointsPerRadius, o->ldA, o->ldB, o->intensityCoeff);
   if (!I->d_lens) {
     I->ck(cudaStreamCreateWithFlags(&I->st, cudaStreamNonBlocking));
-    I->ck(cudaMalloc(&I->d_lens, sizeof(tl::DevLens)));
-    I->ck(cudaMalloc(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen));
-    I->ck(cudaMalloc(&I->d_ca, sizeof(cx) * tl::kBranches * tl::kCCLen));
-    I->ck(cudaMalloc(&I->d_chain, sizeof(tl::RootChain)));
+    I->ck(cudaMallocAsync(&I->d_lens, sizeof(tl::DevLens), I->st));
+    I->ck(cudaMallocAsync(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen, I->st));
+    I->ck(cudaMallocAsync(&I->d_ca, sizeof(cx) * tl::kBranches * tl::kCCLen, I->st));
+    I->ck(cudaMallocAsync(&I->d_chain, sizeof(tl::RootChain), I->st));
   }
-  tl::LensSpec* d_spec = (tl::LensSpec*)I->specbuf.need(sizeof(tl::LensSpec));
+  tl::LensSpec* d_spec = (tl::LensSpec*)I->specbuf.need(sizeof(tl::LensSpec), I->st);
   I->ck(cudaMemcpyAsync(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, I->st));
   tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, I->st);
+  // every copy into pageable host memory waits for its stream first: such a
+  // copy holds the driver's staging path while it waits, and would stall the
+  // copies of every other host thread behind a long kernel
+  I->ck(cudaStreamSynchronize(I->st));
   I->ck(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost, I->st));
   I->ck(cudaStreamSynchronize(I->st));
   // a fresh object's solver: no roots yet, the constructor's heap state
@@ -108,15 +114,19 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
 LightCurveIRS::~LightCurveIRS() {
   tl::Engine::get().trace("delete object");
   if (impl) {
-    cudaFree(impl->d_lens);
-    cudaFree(impl->d_cc);
-    cudaFree(impl->d_ca);
-    cudaFree(impl->d_chain);
-    if (impl->st) cudaStreamDestroy(impl->st);
+    // stream-ordered releases: no wait for work on other streams
+    cudaStream_t st = impl->st;
+    for (void* q : {(void*)impl->d_lens, (void*)impl->d_cc, (void*)impl->d_ca,
+                    (void*)impl->d_chain})
+      if (q) cudaFreeAsync(q, st);
     for (tl::DevBuf* d : {&impl->bufs.trajs, &impl->bufs.jobs, &impl->bufs.scan, &impl->bufs.prep,
                           &impl->bufs.points, &impl->bufs.seeds, &impl->bufs.out,
                           &impl->bufs.trials, &impl->bufs.dump, &impl->specbuf, &impl->ampbuf})
-      if (d->p) cudaFree(d->p);
+      d->release(st);
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
     delete impl;
   }
 }
@@ -183,6 +193,220 @@ void LightCurveIRS::printOutLCParameters() {
   f << "}";
 }
 
+namespace {
+
+// Per-point results of a curve (its n+1 PointOut records) into the object:
+// counts, status, magnifications, statistics, and the reference's per-point
+// stdout lines (lcirs.cc:121-122, 176-177).
+void absorb_results(LightCurveIRS* o, std::complex<double> s, std::complex<double> e,
+                    const tl::PointOut* hout, bool failed) {
+  const uint32_t n = o->lcLength;
+  const size_t np = (size_t)n + 1;
+  o->counts.resize(np);
+  o->status.resize(np);
+  o->diag.resize(np);
+  o->nseeds.resize(np);
+  o->lastStatus = failed ? 0x100u : 0u;
+  o->stats[0] = o->stats[1] = o->stats[2] = 0;
+  const double scale = o->impl->lens.g.amp_scale;
+  for (size_t i = 0; i < np; i++) {
+    o->counts[i] = hout[i].count;
+    o->status[i] = hout[i].status;
+    o->diag[i] = hout[i].diag;
+    o->nseeds[i] = (int32_t)hout[i].nseeds;
+    o->lastStatus |= hout[i].status;
+    o->stats[0] += hout[i].rays_eval;
+    o->stats[1] += hout[i].rays_fp64;
+    o->stats[2] += hout[i].tiles;
+    const double wsum = (double)hout[i].wsum_fx / tl::kWsumScale;
+    o->impl->lcFull[i] = wsum * scale;
+  }
+  for (size_t i = 0; i < n; i++) o->lcVec[i] = o->impl->lcFull[i];
+  if (o->verbose) {
+    std::cout << "IRS called with imgPlaneSize:" << o->impl->lens.g.n << "\n";
+    for (size_t i = 0; i < np; i++) {
+      const double t = double(i) / double(n);
+      const double px = s.real() + (e.real() - s.real()) * t;
+      const double py = s.imag() + (e.imag() - s.imag()) * t;
+      std::cout << "started pos:" << i << ", (" << px << "," << py << ")\n";
+      std::cout << "irs amplification: " << o->impl->lcFull[i] << " and the count "
+                << o->counts[i] << " and amp scale " << scale << "\n";
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dynamic batching of concurrent get_lc_irs calls.
+//
+// The fill kernel is persistent and occupies every SM, so objects that run
+// their own launches from different host threads mostly wait for each
+// other.  Instead, a call queues its request; the first caller that finds no
+// batch running becomes the leader, waits until requests stop arriving (a
+// gap of 3 ms, at most 100 ms), and runs every queued request with its own
+// chain and precision settings as one batch: one seeds launch (a chain per
+// curve) and one fill, on the batcher's stream.  Every caller then finds its
+// results in its object, exactly as a lone call would leave them.  A lone
+// caller pays the 3 ms window once.
+// ---------------------------------------------------------------------------
+struct Request {
+  LightCurveIRS* obj;
+  std::complex<double> s, e;
+  int chain;       // 0: exact chain, else chunk length
+  int precision;
+  bool done = false;
+};
+
+struct Batcher {
+  std::mutex mu;
+  std::condition_variable cv;
+  std::vector<Request*> pending;
+  bool running = false;
+  uint64_t arrivals = 0;
+  cudaStream_t st = nullptr;
+  tl::RunBufs bufs;
+  tl::DevBuf lenses, ca, chains;
+  std::vector<tl::PointOut> hout;
+  std::vector<int32_t> hseeds;
+};
+
+Batcher& batcher() {
+  static Batcher* b = new Batcher();
+  return *b;
+}
+
+// Runs one batch of requests that share chain mode and precision.
+void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
+  tl::Engine& E = tl::Engine::get();
+  if (!B.st) cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking);
+  const int k = (int)reqs.size();
+  const int chain = reqs[0]->chain, precision = reqs[0]->precision;
+  bool failed = false;
+  auto ck = [&](cudaError_t err) {
+    if (err != cudaSuccess) {
+      fprintf(stderr, "liblcirs: CUDA error %s\n", cudaGetErrorString(err));
+      failed = true;
+    }
+  };
+  std::vector<tl::Traj> trajs(k);
+  std::vector<tl::SeedJob> jobs, scan;
+  std::vector<size_t> base(k + 1, 0);
+  for (int i = 0; i < k; i++) {
+    LightCurveIRS* o = reqs[i]->obj;
+    tl::Traj& T = trajs[i];
+    T.x0 = reqs[i]->s.real();
+    T.y0 = reqs[i]->s.imag();
+    T.x1 = reqs[i]->e.real();
+    T.y1 = reqs[i]->e.imag();
+    T.n = o->lcLength;
+    T.lens = i;
+    T.point_base = (int64_t)base[i];
+    const long np = (long)o->lcLength + 1;
+    tl::plan_jobs(&jobs, i, np, chain, i);
+    if (chain <= 0) tl::plan_jobs(&scan, i, np, tl::kChainChunk, -1);
+    base[i + 1] = base[i] + (size_t)np;
+  }
+  const size_t total = base[k];
+  tl::Run R = B.bufs.prepare(total, k, jobs.size(), false, scan.size(), B.st);
+  auto* dl = (tl::DevLens*)B.lenses.need(sizeof(tl::DevLens) * k, B.st);
+  auto* dca = (cx*)B.ca.need(sizeof(cx) * tl::kBranches * tl::kCCLen * k, B.st);
+  auto* dch = (tl::RootChain*)B.chains.need(sizeof(tl::RootChain) * k, B.st);
+  // gather the objects' lenses, caustics and warm-start chains
+  for (int i = 0; i < k; i++) {
+    const LightCurveIRS::Impl* I = reqs[i]->obj->impl;
+    ck(cudaMemcpyAsync(dl + i, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToDevice, B.st));
+    ck(cudaMemcpyAsync(dca + (size_t)i * tl::kBranches * tl::kCCLen, I->d_ca,
+                       sizeof(cx) * tl::kBranches * tl::kCCLen, cudaMemcpyDeviceToDevice, B.st));
+    ck(cudaMemcpyAsync(dch + i, I->d_chain, sizeof(tl::RootChain), cudaMemcpyDeviceToDevice,
+                       B.st));
+  }
+  ck(cudaMemcpyAsync(R.trajs, trajs.data(), sizeof(tl::Traj) * k, cudaMemcpyHostToDevice, B.st));
+  ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+                     cudaMemcpyHostToDevice, B.st));
+  if (chain <= 0) {
+    ck(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+                       cudaMemcpyHostToDevice, B.st));
+    tl::launch_seeds_exact(R.scan_jobs, (int)scan.size(), R.jobs, (int)jobs.size(), R.trajs, dl,
+                           dca, R.points, R.seeds, R.out, R.trials, R.prep, dch, B.st);
+  } else {
+    tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, dl, dca, R.points, R.seeds, R.out,
+                     R.trials, dch, B.st);
+  }
+  {
+    std::lock_guard<std::mutex> g(E.mu);
+    E.fill_on(R, total, dl, precision, B.st);
+  }
+  // the chains go back to their objects
+  for (int i = 0; i < k; i++)
+    ck(cudaMemcpyAsync(reqs[i]->obj->impl->d_chain, dch + i, sizeof(tl::RootChain),
+                       cudaMemcpyDeviceToDevice, B.st));
+  B.hout.resize(total);
+  B.hseeds.resize(total * 2 * tl::kMaxSeeds);
+  ck(cudaStreamSynchronize(B.st));   // before the pageable copies (see setup_object)
+  ck(cudaMemcpyAsync(B.hout.data(), R.out, sizeof(tl::PointOut) * total, cudaMemcpyDeviceToHost,
+                     B.st));
+  ck(cudaMemcpyAsync(B.hseeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * total,
+                     cudaMemcpyDeviceToHost, B.st));
+  ck(cudaStreamSynchronize(B.st));
+  for (int i = 0; i < k; i++) {
+    LightCurveIRS* o = reqs[i]->obj;
+    const size_t np = base[i + 1] - base[i];
+    o->seeds.assign(B.hseeds.begin() + (ptrdiff_t)(base[i] * 2 * tl::kMaxSeeds),
+                    B.hseeds.begin() + (ptrdiff_t)(base[i + 1] * 2 * tl::kMaxSeeds));
+    (void)np;
+    absorb_results(o, reqs[i]->s, reqs[i]->e, B.hout.data() + base[i], failed);
+  }
+}
+
+}  // namespace
+
+void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
+  Batcher& B = batcher();
+  Request r;
+  r.obj = this;
+  r.s = s;
+  r.e = e;
+  r.chain = chainPoints <= 0 ? 0 : chainPoints;
+  r.precision = precision;
+  std::unique_lock<std::mutex> lk(B.mu);
+  B.pending.push_back(&r);
+  B.arrivals++;
+  B.cv.notify_all();
+  while (!r.done) {
+    if (!B.running) {
+      B.running = true;
+      const auto t0 = std::chrono::steady_clock::now();
+      uint64_t seen = B.arrivals;
+      for (;;) {
+        B.cv.wait_for(lk, std::chrono::milliseconds(3));
+        if (B.arrivals == seen ||
+            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(100))
+          break;
+        seen = B.arrivals;
+      }
+      std::vector<Request*> mine, rest;
+      for (Request* q : B.pending)
+        (q->chain == r.chain && q->precision == r.precision ? mine : rest).push_back(q);
+      B.pending.swap(rest);
+      lk.unlock();
+      tl::Engine& E = tl::Engine::get();
+      if (E.tracing) {
+        char msg[96];
+        snprintf(msg, sizeof msg, "batch of %zu curves (%zu left queued)", mine.size(),
+                 B.pending.size());
+        E.trace(msg);
+      }
+      run_batch(B, mine);
+      E.trace("batch done");
+      lk.lock();
+      for (Request* q : mine) q->done = true;
+      B.running = false;
+      B.cv.notify_all();
+    } else {
+      B.cv.wait(lk);
+    }
+  }
+}
+
 void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
                             const int32_t* extSeeds, const int32_t* extN) {
   tl::Engine& E = tl::Engine::get();
@@ -219,6 +443,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   if (extSeeds) {
     // replace the seeds with the caller's, keep the positions
     std::vector<tl::PointOut> hout(np);
+    I->ck(cudaStreamSynchronize(I->st));
     I->ck(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
                             I->st));
     I->ck(cudaStreamSynchronize(I->st));
@@ -246,6 +471,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
     I->ck(cudaStreamSynchronize(I->st));
     E.trace("runFill: fill done");
   }
+  I->ck(cudaStreamSynchronize(I->st));   // before the pageable copies (see setup_object)
   std::vector<tl::PointOut> hout(np);
   I->ck(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
                           I->st));
@@ -270,36 +496,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
                        cudaMemcpyDeviceToHost));
   }
   E.trace("runFill: results copied");
-  counts.resize(np);
-  status.resize(np);
-  diag.resize(np);
-  lastStatus = I->failed ? 0x100u : 0u;
-  stats[0] = stats[1] = stats[2] = 0;
-  const double scale = impl->lens.g.amp_scale;
-  for (size_t i = 0; i < np; i++) {
-    counts[i] = hout[i].count;
-    status[i] = hout[i].status;
-    diag[i] = hout[i].diag;
-    nseeds[i] = (int32_t)hout[i].nseeds;
-    lastStatus |= hout[i].status;
-    stats[0] += hout[i].rays_eval;
-    stats[1] += hout[i].rays_fp64;
-    stats[2] += hout[i].tiles;
-    const double wsum = (double)hout[i].wsum_fx / tl::kWsumScale;
-    impl->lcFull[i] = wsum * scale;
-  }
-  for (size_t i = 0; i < n; i++) lcVec[i] = impl->lcFull[i];
-  if (verbose) {
-    std::cout << "IRS called with imgPlaneSize:" << impl->lens.g.n << "\n";
-    for (size_t i = 0; i < np; i++) {
-      const double t = double(i) / double(n);
-      const double px = s.real() + (e.real() - s.real()) * t;
-      const double py = s.imag() + (e.imag() - s.imag()) * t;
-      std::cout << "started pos:" << i << ", (" << px << "," << py << ")\n";
-      std::cout << "irs amplification: " << impl->lcFull[i] << " and the count " << counts[i]
-                << " and amp scale " << scale << "\n";
-    }
-  }
+  absorb_results(this, s, e, hout.data(), I->failed);
   if (amoebaPrintOut_) {
     // rows of every point from its tile masks: maximal runs, merged across
     // neighbouring tiles (amoeba.cc:90-108 writes "ny,xleft,xright")
@@ -340,8 +537,12 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
 }
 
 void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
-  if (amoebaPrintOut_) printOutLCParameters();
-  runFill(s, e, nullptr, nullptr);
+  if (amoebaPrintOut_) {
+    printOutLCParameters();
+    runFill(s, e, nullptr, nullptr);   // the amoeba dump needs the object's own run
+  } else {
+    runBatched(s, e);
+  }
 }
 
 void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
@@ -362,13 +563,14 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   I->ck(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
   I->ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, I->st));
-  double* d_amp = (double*)I->ampbuf.need(sizeof(double) * n);
+  double* d_amp = (double*)I->ampbuf.need(sizeof(double) * n, I->st);
   if (chainPoints <= 0)
     tl::launch_point_lc_exact(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp,
                               impl->d_chain, I->st);
   else
     tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, impl->d_chain,
                         I->st);
+  I->ck(cudaStreamSynchronize(I->st));   // before the pageable copy (see setup_object)
   I->ck(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
                           I->st));
   I->ck(cudaStreamSynchronize(I->st));
