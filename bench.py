@@ -306,6 +306,81 @@ def surrogate_leg(seed, train_lenses, eval_lenses):
     }
 
 
+def noalloc_leg(lens, traj, n, reps=3):
+    """lcirs_fill_device_noalloc (static 80 MiB scratch, 8 fill CTAs) on one
+    curve's points, with the seeds of the object's own get_lc_irs; counts are
+    compared with that run."""
+    import ctypes
+    import torch
+    from triplelens_gb300.lcirs import LC_irs, load_lcirs
+    L = load_lcirs()
+    fn = L.lcirs_fill_device_noalloc
+    vp = ctypes.c_void_p
+    fn.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
+    fn.restype = ctypes.c_int
+    with quiet_stdout():
+        lc = LC_irs(*lens[:5], lens[5], n, int(lens[7]))
+        lc.set_verbose(0)
+        lc.set_limb_darkening("linear", lens[6])
+        lc.get_lc_irs(*traj)
+    seeds, nseeds = lc.seeds()
+    t = np.arange(n + 1, dtype=np.float64) / float(n)
+    xy = np.stack([traj[0] + (traj[2] - traj[0]) * t, traj[1] + (traj[3] - traj[1]) * t], 1)
+    dev = torch.device("cuda")
+    d_xy = torch.from_numpy(xy).to(dev)
+    d_seeds = torch.from_numpy(np.ascontiguousarray(seeds, np.int32)).to(dev)
+    d_ns = torch.from_numpy(np.ascontiguousarray(nseeds, np.int32)).to(dev)
+    d_mag = torch.zeros(n + 1, dtype=torch.float64, device=dev)
+    d_cnt = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+    args = (vp(lc.obj), n + 1, d_xy.data_ptr(), d_seeds.data_ptr(), d_ns.data_ptr(),
+            d_mag.data_ptr(), d_cnt.data_ptr(), None, vp(stream.cuda_stream))
+    assert fn(*args) == 0
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn(*args)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    cnt = d_cnt.cpu().numpy().view(np.uint64)
+    return {"points": n + 1, "ms_per_call": float(np.median(ms)),
+            "points_per_s": (n + 1) / (float(np.median(ms)) / 1e3),
+            "counts_equal_get_lc_irs": bool(np.array_equal(cnt, lc.counts())),
+            "path": "lcirs_fill_device_noalloc, device arrays, static scratch (8 fill CTAs)"}
+
+
+_T0 = time.perf_counter()
+
+
+def leg(what):
+    """Progress of the bench's legs on stderr (the JSON line stays alone on
+    stdout)."""
+    print("[bench %.1fs] %s" % (time.perf_counter() - _T0, what), file=sys.stderr, flush=True)
+
+
+def child_leg(argv, timeout):
+    """Runs one leg (`bench.py --leg ...`) in a child process on the same GPU
+    and returns its JSON object; a leg that does not finish within `timeout`
+    seconds is killed and reported as such, so the headline line is always
+    printed."""
+    cmd = [sys.executable, os.path.abspath(__file__)] + argv
+    try:
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=None, timeout=timeout,
+                           text=True)
+    except subprocess.TimeoutExpired:
+        return {"unavailable": "did not finish within %d s (child killed)" % timeout}
+    if r.returncode != 0:
+        return {"unavailable": "exited with status %d" % r.returncode}
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    if not lines:
+        return {"unavailable": "printed no result"}
+    return json.loads(lines[-1])
+
+
 def rank_seed(seed, rank):
     """Weak scaling: every rank draws its own curves (independent objects,
     no data-path collective)."""
@@ -386,12 +461,18 @@ def main():
                     help="warm-start chain: 0 = one per curve (the reference's, exact), "
                          "k > 0 = restart every k points")
     ap.add_argument("--cpu-sample", type=int, default=256, help="points timed on the CPU")
-    ap.add_argument("--e2e-threads", type=int, default=64)
+    ap.add_argument("--e2e-threads", type=int, default=0,
+                    help="host threads of the e2e leg (0: one per curve)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fast", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-config4", action="store_true")
+    ap.add_argument("--no-noalloc", action="store_true")
+    ap.add_argument("--leg", choices=["config4", "surrogate"], default=None,
+                    help="run one side leg alone and print its JSON object")
+    ap.add_argument("--leg-timeout", type=int, default=300,
+                    help="seconds allowed to each side leg run as a child process")
     ap.add_argument("--c4-curves", type=int, default=64,
                     help="config-4 sub-sample: curves of 2000 points, each its own lens")
     ap.add_argument("--sur-train-lenses", type=int, default=1024,
@@ -399,6 +480,16 @@ def main():
     ap.add_argument("--sur-eval-lenses", type=int, default=16384,
                     help="surrogate evaluation lenses (64 queries each)")
     args = ap.parse_args()
+
+    if args.leg is not None:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if args.leg == "config4":
+            out = config4_leg(args.seed, args.c4_curves, args.steps)
+        else:
+            out = surrogate_leg(args.seed, args.sur_train_lenses, args.sur_eval_lenses)
+        print(json.dumps(out))
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -513,6 +604,7 @@ def main():
         dist.barrier()
     ms_step = tot_ms / args.steps
     value = npts * world / (ms_step / 1e3)
+    leg("timed steps: %.1f ms per step" % ms_step)
     incomplete = int(np.sum((st & 0xC) != 0))
 
     # the same workload with chunked warm-start chains (parallel seeds)
@@ -538,10 +630,11 @@ def main():
                 "count_mismatches_vs_exact": int(np.sum(fcnt != cnt)),
                 "parity": parity_vs_fixture(fcnt, n, len(lenses), args.seed, rank)}
         del bf
+        leg("chunked-chain leg")
 
     e2e = None
     if not args.no_e2e:
-        threads = max(1, min(len(lenses), args.e2e_threads))
+        threads = len(lenses) if args.e2e_threads <= 0 else min(len(lenses), args.e2e_threads)
         with quiet_stdout():
             e2e_objects(lenses, trajs, n, args.chain, threads)          # warm-up pass
             torch.cuda.synchronize()
@@ -571,6 +664,7 @@ def main():
                             "path": "tlb_set_lenses + tlb_run_host (host buffers in and out)",
                             "counts_equal_device_run": bool(np.array_equal(cntb, cnt))}
         del bh
+        leg("e2e legs")
 
     peaks = measured_peaks()
     clocks = clk.summary(local_rank)
@@ -616,10 +710,21 @@ def main():
         # overflow levels (collect + fill each)
         "gpu_launches": (11 if args.chain <= 0 else 10) * args.steps,
     }
+    if rank == 0 and not args.no_noalloc:
+        line["noalloc"] = noalloc_leg(lenses[0], trajs[0], n)
+        leg("noalloc leg")
     if rank == 0 and not args.no_config4:
-        line["config4"] = config4_leg(args.seed, args.c4_curves, max(1, min(args.steps, 3)))
+        line["config4"] = child_leg(["--leg", "config4", "--seed", str(args.seed),
+                                     "--c4-curves", str(args.c4_curves),
+                                     "--steps", str(max(1, min(args.steps, 3)))],
+                                    args.leg_timeout)
+        leg("config4 leg")
     if rank == 0 and not args.no_surrogate:
-        line["surrogate"] = surrogate_leg(args.seed, args.sur_train_lenses, args.sur_eval_lenses)
+        line["surrogate"] = child_leg(["--leg", "surrogate", "--seed", str(args.seed),
+                                       "--sur-train-lenses", str(args.sur_train_lenses),
+                                       "--sur-eval-lenses", str(args.sur_eval_lenses)],
+                                      args.leg_timeout)
+        leg("surrogate leg")
     if pool is not None and rank == 0:
         pts_s, pts_s1, rays_s, desc, busy = cpu_baseline(pool, ncpu, lenses, trajs, n,
                                                          args.cpu_sample)

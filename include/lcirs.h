@@ -128,8 +128,11 @@ void lcirs_copy_diag(LightCurveIRS* lc, uint32_t* diag);
  * int32); outputs mag (npoints doubles), and optionally counts (uint64) and
  * status (uint32, bits as lcirs_last_status).  The object's lens, grid,
  * limb darkening and precision are used; the current device must be the one
- * the object was created on.  Work is queued on `stream` (a cudaStream_t, NULL
- * for the default stream) and the call returns without waiting.
+ * the object was created on (another current device returns -1 and prints
+ * both device numbers).  Seed counts are clamped to 0..64 (a negative count
+ * fills nothing, a count above 64 uses the 64 stored pixels).  Work is queued
+ * on `stream` (a cudaStream_t, NULL for the default stream) and the call
+ * returns without waiting.
  *
  * Scratch memory is one static device array of 80 MiB, held by every GPU
  * that loads the library's device code until the process exits.  The first

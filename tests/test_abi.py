@@ -100,3 +100,13 @@ def test_entry_points_reject_bad_arguments_without_a_gpu(product_lib):
     assert fn(None, 0, None, None, None, ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0),
               None, None, None, None, None) == -1
     assert lib.tls_param_count() == 16 * 256 + 256 + 3 * (256 * 256 + 256) + 256 + 1
+
+
+def test_static_noalloc_scratch_lives_in_liblcirs_only(product_lib):
+    """The allocation-free entry point's static device array is linked into
+    liblcirs.so alone: a process that loads liblccuda.so as well holds it
+    once."""
+    lcirs = ctypes.CDLL(product_lib)
+    lccuda = ctypes.CDLL(os.path.join(os.path.dirname(product_lib), "liblccuda.so"))
+    assert hasattr(lcirs, "lcirs_fill_device_noalloc")
+    assert not hasattr(lccuda, "lcirs_fill_device_noalloc")

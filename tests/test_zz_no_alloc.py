@@ -126,3 +126,53 @@ def test_noalloc_rejects_too_many_points(product_lib):
            d_mag.data_ptr(), None, None, None)
     assert r == -3
     torch.cuda.synchronize(dev)
+
+
+def test_noalloc_seed_counts_are_clamped(product_lib):
+    """nseeds < 0 fills nothing; nseeds > 64 uses the 64 stored pixels."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from triplelens_gb300.lcirs import load_lcirs
+    fn = _bind(load_lcirs(product_lib))
+    lens, traj, n = workloads.config1()
+    lens = lens.copy()
+    lens[6] = 0.5
+    lc, seeds, nseeds, counts, amps, status = _case(product_lib, lens, traj, n)
+    xy = _positions(traj, n)
+    # every slot past a point's count repeats its first seed pixel, so all 64
+    # stored pixels seed the same components as the first nseeds
+    full = np.array(seeds, dtype=np.int32, copy=True)
+    for i, c in enumerate(nseeds):
+        if 0 < c < 64:
+            full[i, c:] = full[i, 0]
+    mag, cnt, st, _, _ = _run_noalloc(fn, lc, xy, full, np.full(len(xy), 100, np.int32))
+    has = np.asarray(nseeds) > 0
+    assert np.array_equal(cnt[has], counts[has])
+    assert np.max(np.abs(mag[has] - amps[has]) / amps[has]) < LD_RTOL
+    mag, cnt, st, _, _ = _run_noalloc(fn, lc, xy, full, np.full(len(xy), -1, np.int32))
+    assert np.all(cnt == 0) and np.all(mag == 0.0)
+    assert np.all(st & 0x4 == 0)
+
+
+def test_noalloc_table_overflow_sets_status_bit_4(product_lib):
+    """A point whose images need more than the static table's blocks comes
+    back with status bit 4 and a partial count; every other point is exact."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from triplelens_gb300.lcirs import load_lcirs
+    fn = _bind(load_lcirs(product_lib))
+    # the caustic crossing of magnification ~55, at 500 rays per radius:
+    # ~4e7 rays around its images, more than 16384 blocks of 32 x 32
+    lenses, trajs, n = workloads.config2(3, n_curves=1, n_points=64, rho=1e-3, ppr=500)
+    lc, seeds, nseeds, counts, amps, status = _case(product_lib, lenses[0], trajs[0], n)
+    assert int(np.bitwise_or.reduce(status)) & 0x4 == 0   # the allocating fill retries
+    mag, cnt, st, _, _ = _run_noalloc(fn, lc, _positions(trajs[0], n), seeds, nseeds)
+    full = (st & 0x4) != 0
+    assert full.any(), "no point overflowed: max count %d" % int(counts.max())
+    assert np.all(counts[full] > 12288 * 1024 // 2)
+    assert np.all(cnt[full] < counts[full])
+    ok = ~full
+    assert np.array_equal(cnt[ok], counts[ok])
+    assert np.array_equal(st[ok], status[ok])

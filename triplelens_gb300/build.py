@@ -43,8 +43,10 @@ LIBS = {
                     "noalloc_abi.cu", "surrogate.cu"],
     "libccc.so": ["ccc_abi.cu"],
     "libimg.so": ["img_abi.cu"],
+    # without noalloc_abi.cu: its static scratch array stays in liblcirs.so
+    # alone, so a process that loads both libraries holds it once
     "liblccuda.so": ["seeds.cu", "chain.cu", "fill.cu", "engine_host.cu", "lcirs_abi.cu", "batch_abi.cu",
-                     "noalloc_abi.cu", "surrogate.cu", "lccuda_abi.cu"],
+                     "surrogate.cu", "lccuda_abi.cu"],
 }
 
 

@@ -56,6 +56,8 @@ struct RunBufs {
 
 // device copy of an object's lens, grid and limb darkening (lcirs_abi.cu)
 const DevLens* object_device_lens(const LightCurveIRS* lc);
+// the device an object's buffers live on (-1 before its set-up)
+int object_device(const LightCurveIRS* lc);
 
 class Engine {
  public:

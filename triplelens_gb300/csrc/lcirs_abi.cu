@@ -41,6 +41,7 @@ struct LightCurveIRS::Impl {
   // threads set up and seed concurrently; their fills take turns on the
   // engine's tables
   cudaStream_t st = nullptr;
+  int dev = -1;             // the device current when the object was set up
   tl::RunBufs bufs;
   tl::DevBuf specbuf, ampbuf;
   bool failed = false;
@@ -63,6 +64,7 @@ void setup_object(LightCurveIRS* o) {
   I->spec = tl::make_lens_spec(o->a, o->b, o->th, o->m2, o->m3, o->sourceRadius,
                                o->pointsPerRadius, o->ldA, o->ldB, o->intensityCoeff);
   if (!I->d_lens) {
+    I->ck(cudaGetDevice(&I->dev));
     I->ck(cudaStreamCreateWithFlags(&I->st, cudaStreamNonBlocking));
     I->ck(cudaMallocAsync(&I->d_lens, sizeof(tl::DevLens), I->st));
     I->ck(cudaMallocAsync(&I->d_cc, sizeof(cx) * tl::kBranches * tl::kCCLen, I->st));
@@ -582,6 +584,7 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
 // ---------------------------------------------------------------------------
 namespace tl {
 const DevLens* object_device_lens(const LightCurveIRS* lc) { return lc->impl->d_lens; }
+int object_device(const LightCurveIRS* lc) { return lc->impl->dev; }
 }  // namespace tl
 
 extern "C" {

@@ -132,6 +132,17 @@ extern "C" int lcirs_fill_device_noalloc(LightCurveIRS* lc, int npoints, const d
             npoints, kMaxPoints);
     return -3;
   }
+  // the object's lens lives on the device it was created on; launching on
+  // another device would read foreign addresses
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) return -2;
+  if (tl::object_device(lc) != cur) {
+    fprintf(stderr,
+            "lcirs_fill_device_noalloc: the object lives on device %d, the current device is "
+            "%d\n",
+            tl::object_device(lc), cur);
+    return -1;
+  }
   int err = 0;
   char* base = scratch_base(&err);
   if (!base) return err;
