@@ -480,6 +480,10 @@ def main():
     ap.add_argument("--sur-eval-lenses", type=int, default=16384,
                     help="surrogate evaluation lenses (64 queries each)")
     args = ap.parse_args()
+    # a step that stalls shows where: every thread's Python stack on stderr
+    # every 240 s (stdout keeps the one JSON line)
+    import faulthandler
+    faulthandler.dump_traceback_later(240, repeat=True, file=sys.stderr)
 
     if args.leg is not None:
         import torch
@@ -570,9 +574,11 @@ def main():
         bb.run_device(2, sptr)
         return e1
 
+    leg("inputs set: %d points" % npts)
     for _ in range(args.warmup):
         step_device(b)
     torch.cuda.synchronize()
+    leg("warm-up steps")
     amp, cnt, st = b.download(sptr)
     stats = b.stats()
 
@@ -693,7 +699,7 @@ def main():
         "seeds_ms_per_step": ms_step - fill_ms / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": achieved / peak_tf, "traffic": traffic,
-                     "kernel": "fill_kernel (+ overflow retries)",
+                     "kernel": "wfill_kernel (+ fill_kernel for points above its table)",
                      "flop_per_ray": FLOP_PER_RAY, "flop_per_accepted_ray": FLOP_PER_WEIGHT,
                      "peak_source": "2 x 128 FP32 lanes x %d SMs x sm_max_mhz %.0f (MEASURED_PEAKS)"
                                     % (sms, sm_max),
@@ -706,9 +712,9 @@ def main():
         "fast_chain": fast,
         "clocks": clocks,
         # per step: caustic scan, point prep and the chain kernel (or the scan
-        # and the chunked seeds kernel), 3 ordering kernels, the fill, and two
-        # overflow levels (collect + fill each)
-        "gpu_launches": (11 if args.chain <= 0 else 10) * args.steps,
+        # and the chunked seeds kernel), 3 ordering kernels, the warp fill, and
+        # three CTA-fill levels for its overflow (collect + fill each)
+        "gpu_launches": (13 if args.chain <= 0 else 12) * args.steps,
     }
     if rank == 0 and not args.no_noalloc:
         line["noalloc"] = noalloc_leg(lenses[0], trajs[0], n)

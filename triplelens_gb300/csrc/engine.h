@@ -225,4 +225,37 @@ int fill_default_ctas();        // SMs x fill_occupancy()
 void set_fill_occupancy(int occ);  // 2, 3 or 4 resident fill CTAs per SM
 int fill_occupancy();
 
+// ---------------------------------------------------------------------------
+// Warp fill (fill.cu, wfill_kernel): one warp fills one point alone.  Its
+// blocks of 32 x 32 rays live in the warp's own hash table in HBM (key,
+// 16-word header with the entry masks, the filled border and the state, and
+// a 64-word body with the accepted and filled rows); its work stack, queued
+// bitmap, super-tile expansions and seed pixels in shared memory.  No warp
+// waits for another.  Points predicted above `wthr` blocks, and points whose
+// table fills up, come back with status bit 4 for the CTA fill's levels.
+// ---------------------------------------------------------------------------
+constexpr int kWCapLog2 = 14;                 // blocks per warp table (log2)
+constexpr int kWHdrWords = 16;
+struct WScratch {
+  uint64_t* keys;          // [warps << kWCapLog2]
+  uint32_t* hdr;           // [warps << kWCapLog2][kWHdrWords]
+  uint32_t* body;          // [warps << kWCapLog2][64]
+  uint32_t* used;          // [warps << kWCapLog2] slots used by the current point
+  uint32_t* spill;         // [warps << kWCapLog2] work stack beyond its shared part
+  unsigned* next_point;
+  int warps;
+  uint32_t wthr;           // points predicted above this many blocks go to the CTA fill
+  uint32_t* dump;          // optional amoeba export, as FillScratch
+  unsigned* dump_count;
+  unsigned dump_cap;
+};
+int wfill_default_warps();      // SMs x resident warp-fill warps per SM
+size_t wscratch_bytes(int warps);
+void wscratch_init(WScratch* s, void* base, int warps, cudaStream_t st);
+// d_list/d_count (optional): process only the listed points
+void launch_wfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
+                  const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
+                  cudaStream_t st, const int32_t* d_list = nullptr,
+                  const unsigned* d_count = nullptr);
+
 }  // namespace tl

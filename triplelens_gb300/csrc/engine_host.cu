@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 #include "engine_host.h"
 
@@ -80,6 +81,8 @@ Engine::Engine() {
   // TL_FILL_LEVELS=1 disables the overflow retries (and their tables)
   if (const char* c = getenv("TL_FILL_LEVELS")) levels_ = atoi(c);
   if (const char* c = getenv("TL_FILL_PROFILE")) profiling = atoi(c) != 0;
+  if (const char* c = getenv("TL_FILL_KERNEL")) warp_fill_ = std::string(c) == "cta" ? 0 : 1;
+  if (const char* c = getenv("TL_WFILL_THR")) wfill_thr_ = (unsigned)atoi(c);
   if (const char* c = getenv("TL_BLOCK_H")) {
     const int b = atoi(c);
     if (b == 8 || b == 16 || b == 32) block_h_ = b;
@@ -156,6 +159,15 @@ bool Engine::ensure_fill_scratch(int level) {
   return true;
 }
 
+bool Engine::ensure_wscratch() {
+  if (ws_.keys) return true;
+  const int warps = wfill_default_warps();
+  if (!check(cudaMalloc(&wfill_base_, wscratch_bytes(warps)))) return false;
+  wscratch_init(&ws_, wfill_base_, warps, stream);
+  check(cudaStreamSynchronize(stream));
+  return true;
+}
+
 Run RunBufs::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nscan,
                      cudaStream_t st) {
   Run R;
@@ -192,6 +204,7 @@ void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
 
 void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
   if (!ensure_fill_scratch(0)) return;
+  if (warp_fill_ && !ensure_wscratch()) return;
   // the tables are shared: start after the previous fill, on any stream (a
   // graph being captured is ordered at its launch instead)
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -220,8 +233,21 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     cudaHostGetDevicePointer((void**)&heartbeat_dev_, heartbeat_host_, 0);
   }
   s.heartbeat = heartbeat_dev_;
-  launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st, order_list,
-              order_meta);
+  if (warp_fill_) {
+    // one warp per point for every point up to wfill_thr_ predicted blocks;
+    // the larger ones, and those whose warp table fills up, come back with
+    // status bit 4 and go to the CTA fill below (all its levels)
+    WScratch w = ws_;
+    w.wthr = wfill_thr_;
+    w.dump = R.dump;
+    w.dump_count = R.dump_count;
+    w.dump_cap = R.dump_cap;
+    launch_wfill(R.points, (int)np, d_lenses, R.seeds, R.out, w, mode, st, order_list,
+                 order_meta);
+  } else {
+    launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st, order_list,
+                order_meta);
+  }
   if (heartbeat_host_) {
     // a side thread reports the warps' phases while the stream is busy; the
     // caller keeps blocking as usual
@@ -270,9 +296,11 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
   char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
   int32_t* list = (int32_t*)(rb + 64);
   unsigned* count = (unsigned*)rb;
-  for (int level = 1; level < kFillLevels && level < levels_; level++) {
+  for (int level = warp_fill_ ? 0 : 1; level < kFillLevels && level < levels_ + warp_fill_;
+       level++) {
     if (!ensure_fill_scratch(level)) break;
     FillScratch sl = fs_[level];
+    sl.nbig = nullptr;   // a retry list is not size-ordered: every CTA takes from it
     sl.dump = R.dump;
     sl.dump_count = R.dump_count;
     sl.dump_cap = R.dump_cap;

@@ -96,6 +96,13 @@ class Engine {
  private:
   Engine();
   bool ensure_fill_scratch(int level);
+  bool ensure_wscratch();
+  void* wfill_base_ = nullptr;
+  WScratch ws_{};
+  // 1: the warp fill takes every point up to wfill_thr_ predicted blocks and
+  // the CTA fill the rest (TL_FILL_KERNEL=cta: the CTA fill alone)
+  int warp_fill_ = 1;
+  unsigned wfill_thr_ = 7000;
   RunBufs run_;
   DevBuf retry_, prof_, order_;
   cudaEvent_t fill_done_ = nullptr;   // the last fill launched

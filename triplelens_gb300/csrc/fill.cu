@@ -367,8 +367,10 @@ __device__ __forceinline__ double shfl_d(double v, int src) {
   return __shfl_sync(0xffffffffu, v, src);
 }
 
-// whole warp: computes the entry of super-tile (sx, sy) into `ent`
-__device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, int lane, uint32_t* ent) {
+// whole warp: the expansion of super-tile (sx, sy) (every lane leaves with
+// the same values)
+__device__ __noinline__ void supertile_values(const Ctx& c, int sxi, int syi, int lane,
+                                              SuperTile* out) {
   const int half = 1 << (c.slog2 - 1);
   const int64_t nxc = ((int64_t)sxi << c.slog2) + half;
   const int64_t nyc = ((int64_t)syi << c.slog2) + half;
@@ -457,22 +459,57 @@ __device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, i
     mode = kModeExact32;
   }
   const double band = 4.0 * c.rho * E + 4.0 * E * E + 4.0 * u * c.rho2;
+  out->mode = mode;
+  out->K = K;
+  out->d0x = (float)d0x;
+  out->d0y = (float)d0y;
+  out->band = (float)(band * 1.0001);
+  // the exact-difference form keeps W_i (FP32) where the expansion keeps c_n
+  const float w0x = (float)__shfl_sync(0xffffffffu, wx, 0);
+  const float w0y = (float)__shfl_sync(0xffffffffu, wy, 0);
+  const float w1x = (float)__shfl_sync(0xffffffffu, wx, 1);
+  const float w1y = (float)__shfl_sync(0xffffffffu, wy, 1);
+  const float w2x = (float)__shfl_sync(0xffffffffu, wx, 2);
+  const float w2y = (float)__shfl_sync(0xffffffffu, wy, 2);
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    out->cr[n] = mode == kModeTaylor ? cr[n] : 0.f;
+    out->ci[n] = mode == kModeTaylor ? ci[n] : 0.f;
+  }
+  if (mode == kModeExact32) {
+    out->cr[0] = w0x;
+    out->ci[0] = w0y;
+    out->cr[1] = w1x;
+    out->ci[1] = w1y;
+    out->cr[2] = w2x;
+    out->ci[2] = w2y;
+  }
+  out->nxc = (int)nxc;
+  out->nyc = (int)nyc;
+}
+
+// whole warp: computes the entry of super-tile (sx, sy) into `ent`
+__device__ __noinline__ void compute_supertile(const Ctx& c, int sxi, int syi, int lane, uint32_t* ent) {
+  SuperTile v;
+  supertile_values(c, sxi, syi, lane, &v);
   if (lane == 0) {
-    __stcg(&ent[kSMode], (uint32_t)mode);
-    __stcg(&ent[kSK], (uint32_t)K);
-    __stcg(&ent[kSD0x], __float_as_uint((float)d0x));
-    __stcg(&ent[kSD0y], __float_as_uint((float)d0y));
-    __stcg(&ent[kSBand], __float_as_uint((float)(band * 1.0001)));
-    if (mode == kModeTaylor) {
+    __stcg(&ent[kSMode], (uint32_t)v.mode);
+    __stcg(&ent[kSK], (uint32_t)v.K);
+    __stcg(&ent[kSD0x], __float_as_uint(v.d0x));
+    __stcg(&ent[kSD0y], __float_as_uint(v.d0y));
+    __stcg(&ent[kSBand], __float_as_uint(v.band));
+    if (v.mode == kModeTaylor) {
       for (int n = 0; n < 4; n++) {
-        __stcg(&ent[kSC + 2 * n], __float_as_uint(cr[n]));
-        __stcg(&ent[kSC + 2 * n + 1], __float_as_uint(ci[n]));
+        __stcg(&ent[kSC + 2 * n], __float_as_uint(v.cr[n]));
+        __stcg(&ent[kSC + 2 * n + 1], __float_as_uint(v.ci[n]));
       }
     }
-  }
-  if (mode == kModeExact32 && lane < 3) {  // W_i in FP32
-    __stcg(&ent[kSC + 2 * lane], __float_as_uint((float)wx));
-    __stcg(&ent[kSC + 2 * lane + 1], __float_as_uint((float)wy));
+    if (v.mode == kModeExact32) {  // W_i in FP32
+      for (int n = 0; n < 3; n++) {
+        __stcg(&ent[kSC + 2 * n], __float_as_uint(v.cr[n]));
+        __stcg(&ent[kSC + 2 * n + 1], __float_as_uint(v.ci[n]));
+      }
+    }
   }
   __threadfence();
   __syncwarp();
@@ -1146,6 +1183,527 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
     __threadfence();
     __syncthreads();
   }
+}
+
+// ===========================================================================
+// Warp fill.  One warp fills one point alone, points taken from the
+// size-ordered list (largest first).  The point's blocks of 32 x 32 rays sit
+// in the warp's own open-addressing table in HBM; the work stack (spilling
+// into HBM past kWStack entries), the queued bitmap, the last super-tile
+// expansions and the seed pixels in shared memory.  Each visit of a block
+// does what process_block does (classification, closure, weights, edge
+// test), and the warp is the only writer of its table: no atomics on the
+// table and no waits on other warps.  A block's four neighbours are looked
+// up by four groups of 8 lanes, each probing 8 slots with one load.
+// ===========================================================================
+namespace {
+
+constexpr int kWThreads = 128;                   // 4 warps per CTA
+constexpr int kWWarps = kWThreads / 32;
+constexpr int kWOcc = 8;                         // resident CTAs per SM (32 warps)
+constexpr int kWCap = 1 << kWCapLog2;
+constexpr uint32_t kWMask = (uint32_t)kWCap - 1u;
+constexpr int kWStack = 512;                     // work-stack entries in shared memory
+constexpr int kWStCache = 8;                     // super-tile expansions kept per warp
+constexpr unsigned kWUsable = kWCap / 4 * 3;     // table load limit (blocks per point)
+constexpr unsigned kWPopLimit = 16u * kWCap;     // bound on block visits per point
+constexpr int kWProbeIters = 4 * (kWCap / 8 + 2);
+constexpr unsigned kFull = 0xffffffffu;
+// header words
+constexpr int kHEb = 0, kHEt = 1, kHEl = 2, kHEr = 3;   // entry masks: bottom/top row, left/right column
+constexpr int kHFb = 4, kHFt = 5, kHFl = 6, kHFr = 7;   // filled border: row 0, row 31, column 0, column 31
+constexpr int kHState = 8, kHBx = 9, kHBy = 10;
+constexpr uint32_t kWCls = 1u, kWSeed = 2u;             // state: H and F valid; holds a seed pixel
+
+struct WarpSh {
+  Ctx c;
+  SuperTile st[kWStCache];
+  uint64_t sttag[kWStCache];
+  uint32_t stack[kWStack];
+  uint32_t queued[kWCap / 32];
+  int32_t seedx[kMaxSeeds], seedy[kMaxSeeds];
+  unsigned top, used, nseed;
+};
+
+struct WTable {
+  uint64_t* keys;
+  uint32_t* hdr;
+  uint32_t* body;
+  uint32_t* used;
+  uint32_t* spill;
+};
+
+struct WAcc {
+  unsigned long long count, eval, fp64;
+  long long fx;       // weight sum, units of 2^-16 (lane 0's value is used)
+  unsigned edge;
+};
+
+// one lane: queue `slot` unless it is queued already
+__device__ __forceinline__ void w_queue(WarpSh& W, const WTable& T, uint32_t slot) {
+  const uint32_t bit = 1u << (slot & 31u);
+  if (atomicOr(&W.queued[slot >> 5], bit) & bit) return;
+  const unsigned pos = atomicAdd(&W.top, 1u);
+  if (pos < (unsigned)kWStack) W.stack[pos] = slot;
+  else __stcg(&T.spill[pos], slot);   // pos < number of queued slots <= kWCap
+}
+
+// Whole warp.  The 8 lanes of group g = lane / 8 look up block (bx, by) when
+// `act` (uniform in the group) and insert it when absent; every lane of the
+// group returns the slot (-1: inactive, or no free slot) and *ins = inserted
+// now.  Groups that pick the same free slot in one round: the lower group
+// takes it, the other reads its window again.
+__device__ __noinline__ int w_find4(const WTable& T, bool act, int bx, int by, int lane,
+                                    bool* ins) {
+  const int g = lane >> 3, j = lane & 7;
+  const uint64_t key = tile_key(bx, by);
+  const uint32_t h0 = hash_key(key) & kWMask;
+  int slot = -1;
+  bool done = !act, inserted = false;
+  uint32_t r = 0;
+  for (int it = 0; it < kWProbeIters; it++) {
+    const bool live = !done;
+    if (!__any_sync(kFull, live)) break;
+    const uint32_t base = h0 + r * 8u;
+    uint64_t k = 0;
+    if (live) k = ldcg64(&T.keys[(base + (uint32_t)j) & kWMask]);
+    const uint32_t mm = __ballot_sync(kFull, live && k == key);
+    const uint32_t me = __ballot_sync(kFull, live && k == kEmptyKey);
+    const uint32_t gm = (mm >> (8 * g)) & 0xffu, ge = (me >> (8 * g)) & 0xffu;
+    uint32_t want = kFull;
+    if (live && gm == 0u && ge != 0u) want = (base + (uint32_t)(__ffs(ge) - 1)) & kWMask;
+    const uint32_t w0 = __shfl_sync(kFull, want, 0);
+    const uint32_t w1 = __shfl_sync(kFull, want, 8);
+    const uint32_t w2 = __shfl_sync(kFull, want, 16);
+    const bool lose = want != kFull && ((g > 0 && want == w0) || (g > 1 && want == w1) ||
+                                        (g > 2 && want == w2));
+    bool take = false;
+    if (live) {
+      if (gm != 0u) {
+        slot = (int)((base + (uint32_t)(__ffs(gm) - 1)) & kWMask);
+        done = true;
+      } else if (want != kFull) {
+        if (!lose) {
+          slot = (int)want;
+          inserted = true;
+          take = true;
+          done = true;
+        }
+      } else {
+        r++;
+        if (r > kWMask / 8u) done = true;   // every window holds other keys: no slot
+      }
+    }
+    if (take && j == 0) __stcg((unsigned long long*)&T.keys[slot], (unsigned long long)key);
+    __syncwarp();
+  }
+  *ins = inserted;
+  return slot;
+}
+
+// group of 8 lanes: header of a slot inserted now (entries and border zero),
+// and its place in the used list
+__device__ __forceinline__ void w_init_slot(WarpSh& W, const WTable& T, int slot, int bx, int by,
+                                            int lane) {
+  const int j = lane & 7;
+  uint32_t* h = T.hdr + (size_t)slot * kWHdrWords;
+  for (int q = j; q < kWHdrWords; q += 8)
+    __stcg(&h[q], q == kHBx ? (uint32_t)bx : (q == kHBy ? (uint32_t)by : 0u));
+  if (j == 0) {
+    const unsigned u = atomicAdd(&W.used, 1u);
+    if (u < (unsigned)kWCap) __stcg(&T.used[u], (uint32_t)slot);
+  }
+}
+
+// whole warp: cache index of the expansion of the super-tile holding block
+// (bx, by), computed on a miss
+__device__ __noinline__ int w_supertile(WarpSh& W, int bx, int by, int lane) {
+  const int sh = W.c.slog2 - 5;
+  const int sxi = bx >> sh, syi = by >> sh;
+  const uint64_t key = tile_key(sxi, syi);
+  const int idx = (int)(hash_key(key) & (uint32_t)(kWStCache - 1));
+  if (W.sttag[idx] != key) {
+    SuperTile v;
+    supertile_values(W.c, sxi, syi, lane, &v);
+    __syncwarp();
+    if (lane == 0) {
+      W.st[idx] = v;
+      W.sttag[idx] = key;
+    }
+    __syncwarp();
+  }
+  return idx;
+}
+
+// whole warp: one visit of the block in `slot`
+__device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, int lane,
+                                     WAcc& A) {
+  const Ctx& c = W.c;
+  uint32_t* hdr = T.hdr + (size_t)slot * kWHdrWords;
+  uint32_t* body = T.body + (size_t)slot * 64;
+  const uint32_t hw = lane < kWHdrWords ? ldcg32(&hdr[lane]) : 0u;
+  const uint32_t hb = ldcg32(&body[lane]);
+  const uint32_t fb = ldcg32(&body[32 + lane]);
+  const uint32_t eb = __shfl_sync(kFull, hw, kHEb), et = __shfl_sync(kFull, hw, kHEt);
+  const uint32_t el = __shfl_sync(kFull, hw, kHEl), er = __shfl_sync(kFull, hw, kHEr);
+  const uint32_t state = __shfl_sync(kFull, hw, kHState);
+  const int bx = (int)__shfl_sync(kFull, hw, kHBx), by = (int)__shfl_sync(kFull, hw, kHBy);
+  const bool cls = (state & kWCls) != 0u;
+  uint32_t h_row = cls ? hb : 0u;
+  const uint32_t f_cur = cls ? fb : 0u;
+  uint32_t e_row = (lane == 0 ? eb : 0u) | (lane == 31 ? et : 0u) | ((el >> lane) & 1u) |
+                   (((er >> lane) & 1u) << 31);
+  // seed pixels of this block (lcirs.cc:171-174), applied on every visit
+  if (state & kWSeed) {
+    for (unsigned k = 0; k < W.nseed; k++) {
+      const int32_t px = W.seedx[k], py = W.seedy[k];
+      if ((px >> 5) == bx && (py >> 5) == by && (py & 31) == lane) e_row |= 1u << (px & 31);
+    }
+  }
+  bool fresh = false;
+  float wall = 0.f;
+  int sti = -1;
+  if (!cls) {
+    unsigned nr = 0, n64 = 0;
+    if (c.split) sti = w_supertile(W, bx, by, lane);
+    if (sti >= 0 && W.st[sti].mode != kModeFp64) {
+      const SuperTile stc = W.st[sti];   // by value: the coefficients stay in registers
+      const int K = stc.mode == kModeTaylor ? stc.K : 0;
+      if (K == 0) h_row = classify_block<32, 0>(c, stc, bx, by, lane, &wall, &nr, &n64);
+      else if (K <= 2) h_row = classify_block<32, 2>(c, stc, bx, by, lane, &wall, &nr, &n64);
+      else h_row = classify_block<32, 4>(c, stc, bx, by, lane, &wall, &nr, &n64);
+    } else {
+      h_row = classify_block_fp64<32>(c, bx, by, lane, &wall, &nr, &n64);
+    }
+    A.eval += warp_sum_u(nr);
+    A.fp64 += warp_sum_u(n64);
+    fresh = true;
+  }
+  const uint32_t hp = h_row & ~f_cur;   // accepted, not yet filled
+  uint32_t f = e_row & hp;
+  uint32_t f_new = f_cur;
+  const bool any = __ballot_sync(kFull, f != 0u) != 0u;
+  uint32_t top = 0, bot = 0, lcol = 0, rcol = 0;
+  if (any) {
+    // closure inside the block (as process_block)
+    for (int it = 0; it < 1024; it++) {
+      uint32_t below = __shfl_up_sync(kFull, f, 1);
+      uint32_t above = __shfl_down_sync(kFull, f, 1);
+      if (lane == 0) below = 0u;
+      if (lane == 31) above = 0u;
+      const uint32_t nf = run_fill(f | ((below | above) & hp), hp);
+      const unsigned changed = __ballot_sync(kFull, nf != f);
+      f = nf;
+      if (!changed) break;
+    }
+    f_new = f_cur | f;
+    // weights of the newly filled rays: the whole block when this visit
+    // filled all of its accepted rays at its evaluation, else ray by ray
+    float acc;
+    const bool all = fresh && __ballot_sync(kFull, f != h_row) == 0u;
+    if (all) {
+      acc = wall;
+    } else {
+      acc = 0.f;
+      unsigned re = 0;
+      if (c.split && sti < 0) sti = w_supertile(W, bx, by, lane);
+      const SuperTile stw = sti >= 0 ? W.st[sti] : SuperTile{};
+      const int64_t nx = (int64_t)bx * 32 + lane;
+#pragma unroll 1
+      for (int r = 0; r < 32; r++) {
+        const uint32_t nwr = __shfl_sync(kFull, f, r);
+        if ((nwr >> lane) & 1u) {
+          acc += weight_again(c, stw, c.split && sti >= 0, nx, (int64_t)by * 32 + r);
+          re++;
+        }
+      }
+      A.eval += warp_sum_u(re);
+    }
+    A.count += warp_sum_u(__popc(f));
+    // a block's sum is below 1024 * 1.5: 2^-16 resolution fits an int32
+    A.fx += (long long)__float2int_rn(warp_sum_f(acc) * 65536.f);
+    // plane edge: columns 1 and N-1 (lcirs.cc:413-440)
+    {
+      const int64_t c0 = (int64_t)bx * 32;
+      uint32_t colmask = 0;
+      if (1 >= c0 && 1 < c0 + 32) colmask |= 1u << (1 - c0);
+      if (c.n - 1 >= c0 && c.n - 1 < c0 + 32) colmask |= 1u << (c.n - 1 - c0);
+      if (__reduce_or_sync(kFull, f) & colmask) A.edge = 1u;
+    }
+    top = __shfl_sync(kFull, f, 31);
+    bot = __shfl_sync(kFull, f, 0);
+    lcol = __ballot_sync(kFull, f & 1u);
+    rcol = __ballot_sync(kFull, f >> 31);
+  }
+  // write back: rows, entries consumed, filled border, state (a first visit
+  // writes F as well: the body still holds an earlier point's rows)
+  if (fresh) __stcg(&body[lane], h_row);
+  if (any || fresh) __stcg(&body[32 + lane], f_new);
+  const uint32_t flb = __ballot_sync(kFull, f_new & 1u), frb = __ballot_sync(kFull, f_new >> 31);
+  const uint32_t fr0 = __shfl_sync(kFull, f_new, 0), fr31 = __shfl_sync(kFull, f_new, 31);
+  if (lane <= kHState) {
+    uint32_t v = 0u;
+    if (lane == kHFb) v = fr0;
+    else if (lane == kHFt) v = fr31;
+    else if (lane == kHFl) v = flb;
+    else if (lane == kHFr) v = frb;
+    else if (lane == kHState) v = state | kWCls;
+    __stcg(&hdr[lane], v);
+  }
+  __syncwarp();
+  if (!any) return;
+  // neighbours: group 0 the block above (its bottom row), 1 below (its top
+  // row), 2 left (its column 31), 3 right (its column 0)
+  const int g = lane >> 3, j = lane & 7;
+  int nbx = bx, nby = by, ew, fw;
+  uint32_t bits;
+  if (g == 0) { nby = by + 1; bits = top; ew = kHEb; fw = kHFb; }
+  else if (g == 1) { nby = by - 1; bits = bot; ew = kHEt; fw = kHFt; }
+  else if (g == 2) { nbx = bx - 1; bits = lcol; ew = kHEr; fw = kHFr; }
+  else { nbx = bx + 1; bits = rcol; ew = kHEl; fw = kHFl; }
+  const bool act = bits != 0u && nbx >= 0 && nby >= 0 && nbx <= c.txmax && nby <= c.tymax;
+  bool ins = false;
+  const int s = w_find4(T, act, nbx, nby, lane, &ins);
+  if (s >= 0 && ins) w_init_slot(W, T, s, nbx, nby, lane);
+  __syncwarp();
+  if (s >= 0 && j == 0) {
+    uint32_t* nh = T.hdr + (size_t)s * kWHdrWords;
+    const uint32_t filled = ins ? 0u : ldcg32(&nh[fw]);
+    const uint32_t old = ins ? 0u : ldcg32(&nh[ew]);
+    const uint32_t nb = bits & ~filled;
+    if (nb) {
+      __stcg(&nh[ew], old | nb);
+      w_queue(W, T, (uint32_t)s);
+    }
+  }
+  __syncwarp();
+}
+
+}  // namespace
+
+template <int MINB>
+__global__ void __launch_bounds__(kWThreads, MINB)
+wfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int32_t* seeds,
+             PointOut* out, WScratch sc, int split_mode, const int32_t* list,
+             const unsigned* list_count) {
+  __shared__ WarpSh wsh[kWWarps];
+  const int lane = threadIdx.x & 31;
+  WarpSh& W = wsh[threadIdx.x >> 5];
+  const size_t gw = (size_t)blockIdx.x * kWWarps + (threadIdx.x >> 5);
+  if (gw >= (size_t)sc.warps) return;   // whole warps; the kernel has no block barrier
+  WTable T;
+  T.keys = sc.keys + (gw << kWCapLog2);
+  T.hdr = sc.hdr + (gw << kWCapLog2) * kWHdrWords;
+  T.body = sc.body + (gw << kWCapLog2) * 64;
+  T.used = sc.used + (gw << kWCapLog2);
+  T.spill = sc.spill + (gw << kWCapLog2);
+  const unsigned nwork = list ? *list_count : (unsigned)npoints;
+  for (int i = lane; i < kWCap / 32; i += 32) W.queued[i] = 0u;
+  __syncwarp();
+  for (;;) {
+    unsigned w = 0;
+    if (lane == 0) w = atomicAdd(sc.next_point, 1u);
+    w = __shfl_sync(kFull, w, 0);
+    if (w >= nwork) break;
+    const int p = list ? list[w] : (int)w;
+    const PointIn pi = points[p];
+    if (lane == 0) {
+      const DevLens& D = lenses[pi.lens];
+      Ctx& c = W.c;
+      c.sx = pi.sx;
+      c.sy = pi.sy;
+      c.cx0 = D.g.corner_x;
+      c.cy0 = D.g.corner_y;
+      c.h = D.g.h;
+      c.n = D.g.n;
+      c.rho = D.rho;
+      c.rho2 = D.rho2;
+      c.ld_a = D.ld_a;
+      c.ld_b = D.ld_b;
+      c.m1 = D.L.m1;
+      c.m2 = D.L.m2;
+      c.m3 = D.L.m3;
+      c.z2x = D.L.z2.re;
+      c.z3x = D.L.z3.re;
+      c.z3y = D.L.z3.im;
+      c.binary = D.ray_binary;
+      c.txmax = (int)((c.n - 1) >> 5);
+      c.tymax = (int)((c.n - 1) >> 5);
+      c.split = split_mode;
+      // super-tile edge as the CTA fill: 2^9 pixels, down to 2^7 as h grows
+      int sl = 9;
+      while (sl > 7 && c.h * (double)(1 << sl) > 1.5e-3) sl--;
+      c.slog2 = sl;
+      c.hf = (float)c.h;
+      c.rho2f = (float)c.rho2;
+      c.inv_rho2f = (float)(1.0 / c.rho2);
+      c.ldaf = (float)c.ld_a;
+      c.ldbf = (float)c.ld_b;
+      W.top = 0;
+      W.used = 0;
+      W.nseed = 0;
+    }
+    if (lane < kWStCache) W.sttag[lane] = kEmptyKey;
+    __syncwarp();
+    const int64_t n = W.c.n;
+    uint32_t status = 0;
+    if (!(n > 2 && n < ((int64_t)1 << 31)) || (out[p].status & kStBadInput)) status |= kStBadInput;
+    else if (pi.est_blocks > sc.wthr) status |= kStTableFull;   // left to the CTA fill
+    WAcc A = {0ull, 0ull, 0ull, 0ll, 0u};
+    unsigned pops = 0;
+    if (!status) {
+      // seeds (lcirs.cc:171-174; seed rows must satisfy 0 < ny < N, 386-391)
+      const unsigned ns = min(out[p].nseeds, (unsigned)kMaxSeeds);
+      for (unsigned k0 = 0; k0 < ns; k0 += 32) {
+        const unsigned k = k0 + (unsigned)lane;
+        int32_t px = 0, py = 0;
+        bool ok = false, edge = false;
+        if (k < ns) {
+          px = seeds[((size_t)p * kMaxSeeds + k) * 2];
+          py = seeds[((size_t)p * kMaxSeeds + k) * 2 + 1];
+          if (py > 0 && (int64_t)py < n) {
+            if (px < 1 || (int64_t)px > n - 1) edge = true;
+            else ok = true;
+          }
+        }
+        if (__any_sync(kFull, edge)) status |= kStEdge;
+        const uint32_t okm = __ballot_sync(kFull, ok);
+        if (ok) {
+          const unsigned pos = W.nseed + (unsigned)__popc(okm & ((1u << lane) - 1u));
+          W.seedx[pos] = px;
+          W.seedy[pos] = py;
+        }
+        __syncwarp();
+        if (lane == 0) W.nseed += (unsigned)__popc(okm);
+        __syncwarp();
+      }
+      // seed blocks: found or inserted by group 0, marked and queued
+      const unsigned nsd = W.nseed;
+      for (unsigned k = 0; k < nsd; k++) {
+        const int sbx = W.seedx[k] >> 5, sby = W.seedy[k] >> 5;
+        bool ins = false;
+        const int s = w_find4(T, lane < 8, sbx, sby, lane, &ins);
+        if (lane < 8 && s >= 0 && ins) w_init_slot(W, T, s, sbx, sby, lane);
+        __syncwarp();
+        if (lane == 0 && s >= 0) {
+          uint32_t* h = T.hdr + (size_t)s * kWHdrWords;
+          __stcg(&h[kHState], ldcg32(&h[kHState]) | kWSeed);
+          w_queue(W, T, (uint32_t)s);
+        }
+        __syncwarp();
+        const int sl0 = __shfl_sync(kFull, s, 0);
+        if (sl0 < 0 || W.used > kWUsable) {
+          status |= kStTableFull;
+          break;
+        }
+      }
+      // blocks, last queued first
+      while (!(status & (kStTableFull | kStTimeout))) {
+        const unsigned t = W.top;
+        if (t == 0u) break;
+        const uint32_t slot = t - 1u < (unsigned)kWStack ? W.stack[t - 1u] : ldcg32(&T.spill[t - 1u]);
+        __syncwarp();
+        if (lane == 0) {
+          W.top = t - 1u;
+          W.queued[slot >> 5] &= ~(1u << (slot & 31u));
+        }
+        __syncwarp();
+        w_block(W, T, slot, lane, A);
+        if (W.used > kWUsable) status |= kStTableFull;
+        if (++pops > kWPopLimit) status |= kStTimeout;
+      }
+    }
+    const unsigned nused = min(W.used, (unsigned)kWCap);
+    if (lane == 0) {
+      PointOut o = out[p];
+      o.count = A.count;
+      o.wsum_fx = A.fx * 65536ll;
+      o.status |= status | (A.edge ? (uint32_t)kStEdge : 0u);
+      o.tiles = nused;
+      o.diag = (status & kStTimeout) ? 0x10000u : 0u;
+      o.rays_eval = A.eval;
+      o.rays_fp64 = A.fp64;
+      out[p] = o;
+    }
+    // amoeba export (32 x 8 tiles of F, as the CTA fill) and the clearing
+    // of the slots used (the table starts every point empty)
+    const bool complete = !(status & (kStTableFull | kStTimeout | kStBadInput));
+    for (unsigned u = (unsigned)lane; u < nused; u += 32) {
+      const uint32_t slot = ldcg32(&T.used[u]);
+      if (sc.dump && complete) {
+        const uint32_t* h = T.hdr + (size_t)slot * kWHdrWords;
+        if (ldcg32(&h[kHState]) & kWCls) {
+          const uint32_t* b = T.body + (size_t)slot * 64;
+          const uint32_t bxk = ldcg32(&h[kHBx]), byk = ldcg32(&h[kHBy]);
+          for (int t8 = 0; t8 < 4; t8++) {
+            uint32_t fm[8], a8 = 0;
+            for (int r = 0; r < 8; r++) a8 |= (fm[r] = ldcg32(&b[32 + 8 * t8 + r]));
+            if (!a8) continue;
+            const unsigned d = atomicAdd(sc.dump_count, 1u);
+            if (d < sc.dump_cap) {
+              uint32_t* o = sc.dump + (size_t)d * kDumpWords;
+              o[0] = (uint32_t)p;
+              o[1] = bxk;
+              o[2] = byk * 4u + (uint32_t)t8;
+              for (int r = 0; r < 8; r++) o[3 + r] = fm[r];
+            }
+          }
+        }
+      }
+      __stcg((unsigned long long*)&T.keys[slot], (unsigned long long)kEmptyKey);
+    }
+    // slots left queued by a point given up on
+    if (W.top != 0u)
+      for (int i = lane; i < kWCap / 32; i += 32) W.queued[i] = 0u;
+    __syncwarp();
+  }
+}
+
+int wfill_default_warps() {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms * kWOcc * kWWarps;
+}
+
+size_t wscratch_bytes(int warps) {
+  const size_t ent = (size_t)warps << kWCapLog2;
+  return ent * (8 + (size_t)kWHdrWords * 4 + 64 * 4 + 4 + 4) + 256;
+}
+
+void wscratch_init(WScratch* s, void* base, int warps, cudaStream_t st) {
+  const size_t ent = (size_t)warps << kWCapLog2;
+  char* p = (char*)base;
+  s->warps = warps;
+  s->keys = (uint64_t*)p;
+  p += ent * 8;
+  s->hdr = (uint32_t*)p;
+  p += ent * (size_t)kWHdrWords * 4;
+  s->body = (uint32_t*)p;
+  p += ent * 64 * 4;
+  s->used = (uint32_t*)p;
+  p += ent * 4;
+  s->spill = (uint32_t*)p;
+  p += ent * 4;
+  s->next_point = (unsigned*)p;
+  s->wthr = 7000;
+  s->dump = nullptr;
+  s->dump_count = nullptr;
+  s->dump_cap = 0;
+  // keys empty (all ones); headers are written when a slot is taken, bodies
+  // are read only once their state says so
+  cudaMemsetAsync(s->keys, 0xff, ent * 8, st);
+  cudaMemsetAsync(s->next_point, 0, 256, st);
+}
+
+void launch_wfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
+                  const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
+                  cudaStream_t st, const int32_t* d_list, const unsigned* d_count) {
+  if (npoints <= 0 || s.warps <= 0) return;
+  cudaMemsetAsync(s.next_point, 0, sizeof(unsigned), st);
+  const int ctas = (s.warps + kWWarps - 1) / kWWarps;
+  wfill_kernel<kWOcc><<<ctas, kWThreads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
+                                                  mode == kFillSplit ? 1 : 0, d_list, d_count);
 }
 
 int block_rec_words(int bh) {
