@@ -109,9 +109,11 @@ void lcirs_set_precision(LightCurveIRS* lc, int mode);
  * bits of the warm start. */
 void lcirs_set_chain(LightCurveIRS* lc, int points);
 
-/* Fill-kernel diagnostics of the last get_lc_irs, n+1 entries: bits 0-15
- * the largest number of passes over one tile, bit 16 pass limit reached,
- * bit 17 dequeue limit reached, bits 24-31 the tile state seen then. */
+/* Fill diagnostics of the last get_lc_irs, n+1 entries, from the fill stage
+ * that completed the point: team fill: bits 0-15 its rounds; CTA fill: bits
+ * 0-15 the largest number of passes over one tile, bit 17 dequeue limit
+ * reached, bits 24-31 the tile state seen then; warp fill: 0.  Bit 16: a
+ * bound on passes, visits or rounds was reached. */
 void lcirs_copy_diag(LightCurveIRS* lc, uint32_t* diag);
 
 /* No counterpart in the reference.  Fill-only run that allocates no device

@@ -229,29 +229,50 @@ int fill_occupancy();
 // Warp fill (fill.cu, wfill_kernel): one warp fills one point alone.  Its
 // blocks of 32 x 32 rays live in the warp's own hash table in HBM (key,
 // 16-word header with the entry masks, the filled border and the state, and
-// a 64-word body with the accepted and filled rows); its work stack, queued
-// bitmap, super-tile expansions and seed pixels in shared memory.  No warp
-// waits for another.  Points predicted above `wthr` blocks, and points whose
-// table fills up, come back with status bit 4 for the CTA fill's levels.
+// a 64-word body with the accepted and filled rows); its work stack,
+// super-tile expansions and seed pixels in shared memory.  No warp waits for
+// another.  Points predicted above `wthr` blocks, and points whose table
+// fills up, come back with status bit 4 for the CTA fill's levels.
 // ---------------------------------------------------------------------------
-constexpr int kWCapLog2 = 14;                 // blocks per warp table (log2)
+constexpr int kWCapLog2 = 16;                 // largest warp table (log2 of its slots)
+constexpr int kWCapLog2Min = 10;
 constexpr int kWHdrWords = 16;
 struct WScratch {
-  uint64_t* keys;          // [warps << kWCapLog2]
-  uint32_t* hdr;           // [warps << kWCapLog2][kWHdrWords]
-  uint32_t* body;          // [warps << kWCapLog2][64]
-  uint32_t* used;          // [warps << kWCapLog2] slots used by the current point
-  uint32_t* spill;         // [warps << kWCapLog2] work stack beyond its shared part
+  uint64_t* keys;          // [warps << cap_log2]
+  uint32_t* hdr;           // [warps << cap_log2][kWHdrWords]
+  uint32_t* body;          // [warps << cap_log2][64]
+  uint32_t* used;          // [warps << cap_log2] slots used by the current point
+  uint32_t* spill;         // [warps << cap_log2] work stack beyond its shared part
   unsigned* next_point;
   int warps;
+  int cap_log2;            // slots per warp table (log2), kWCapLog2Min..kWCapLog2
   uint32_t wthr;           // points predicted above this many blocks go to the CTA fill
   uint32_t* dump;          // optional amoeba export, as FillScratch
   unsigned* dump_count;
   unsigned dump_cap;
+  // optional counters (8 x u64): block visits, first visits, super-tile
+  // expansions computed, probe rounds, slots inserted, visits filled whole
+  // by the simple-region test, visits with ray-by-ray weights, points
+  unsigned long long* prof;
+  // team fill only: message inboxes [teams][2][8][inbox_cap]
+  uint4* inbox;
+  unsigned inbox_cap;
 };
 int wfill_default_warps();      // SMs x resident warp-fill warps per SM
-size_t wscratch_bytes(int warps);
-void wscratch_init(WScratch* s, void* base, int warps, cudaStream_t st);
+size_t wscratch_bytes(int warps, int cap_log2);
+void wscratch_init(WScratch* s, void* base, int warps, int cap_log2, cudaStream_t st);
+// Team fill (fill.cu, tfill_kernel): 8 warps of a CTA fill one large point
+// in rounds; each warp owns the blocks of its share of the super-tiles (its
+// own table, laid out as the warp fill's: teams x 8 tables) and sends the
+// entries into other shares as messages, read at the next round.
+int tfill_default_teams();      // 2 per SM
+size_t tscratch_bytes(int teams, int cap_log2, unsigned inbox_cap);
+void tscratch_init(WScratch* s, void* base, int teams, int cap_log2, unsigned inbox_cap,
+                   cudaStream_t st);
+void launch_tfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
+                  const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
+                  cudaStream_t st, const int32_t* d_list = nullptr,
+                  const unsigned* d_count = nullptr);
 // d_list/d_count (optional): process only the listed points
 void launch_wfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                   const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,

@@ -78,11 +78,25 @@ Engine::Engine() {
   if (const char* c = getenv("TL_FILL_OCC")) set_fill_occupancy(atoi(c));
   // TL_FILL_BIG: CTAs with the large level-0 tables (0: none)
   if (const char* c = getenv("TL_FILL_BIG")) want_big_ctas_ = atoi(c);
-  // TL_FILL_LEVELS=1 disables the overflow retries (and their tables)
+  // TL_FILL_LEVELS: CTA-fill table levels used (1: the warp fill's overflow
+  // goes to level 0 only; with TL_FILL_KERNEL=cta, no retries)
   if (const char* c = getenv("TL_FILL_LEVELS")) levels_ = atoi(c);
   if (const char* c = getenv("TL_FILL_PROFILE")) profiling = atoi(c) != 0;
   if (const char* c = getenv("TL_FILL_KERNEL")) warp_fill_ = std::string(c) == "cta" ? 0 : 1;
   if (const char* c = getenv("TL_WFILL_THR")) wfill_thr_ = (unsigned)atoi(c);
+  // TL_WFILL_WARPS: warps of the warp fill (default 32 per SM; each owns a
+  // 5.5 MB table)
+  if (const char* c = getenv("TL_WFILL_WARPS")) want_wfill_warps_ = atoi(c);
+  // TL_TEAM_FILL=0: no team fill (the CTA fill takes the warp fill's leftovers);
+  // TL_TEAMS: teams of 8 warps (default 2 per SM)
+  if (const char* c = getenv("TL_TEAM_FILL")) team_fill_ = atoi(c) != 0;
+  if (const char* c = getenv("TL_TEAMS")) want_teams_ = atoi(c);
+  // TL_WFILL_CAP_LOG2: slots per warp table (10..14; the threshold follows)
+  if (const char* c = getenv("TL_WFILL_CAP_LOG2")) {
+    wfill_cap_log2_ = atoi(c);
+    if (!getenv("TL_WFILL_THR"))
+      wfill_thr_ = (unsigned)(0.43 * (double)(1u << (wfill_cap_log2_ < 10 ? 10 : wfill_cap_log2_)));
+  }
   if (const char* c = getenv("TL_BLOCK_H")) {
     const int b = atoi(c);
     if (b == 8 || b == 16 || b == 32) block_h_ = b;
@@ -161,9 +175,22 @@ bool Engine::ensure_fill_scratch(int level) {
 
 bool Engine::ensure_wscratch() {
   if (ws_.keys) return true;
-  const int warps = wfill_default_warps();
-  if (!check(cudaMalloc(&wfill_base_, wscratch_bytes(warps)))) return false;
-  wscratch_init(&ws_, wfill_base_, warps, stream);
+  const int warps = want_wfill_warps_ > 0 ? want_wfill_warps_ : wfill_default_warps();
+  int cap = wfill_cap_log2_;
+  cap = cap < kWCapLog2Min ? kWCapLog2Min : (cap > kWCapLog2 ? kWCapLog2 : cap);
+  if (!check(cudaMalloc(&wfill_base_, wscratch_bytes(warps, cap)))) return false;
+  wscratch_init(&ws_, wfill_base_, warps, cap, stream);
+  check(cudaStreamSynchronize(stream));
+  return true;
+}
+
+bool Engine::ensure_tscratch() {
+  if (ts_.keys) return true;
+  const int teams = want_teams_ > 0 ? want_teams_ : tfill_default_teams();
+  const int cap = kTeamCapLog2;
+  const unsigned inbox = 1u << 14;
+  if (!check(cudaMalloc(&tfill_base_, tscratch_bytes(teams, cap, inbox)))) return false;
+  tscratch_init(&ts_, tfill_base_, teams, cap, inbox, stream);
   check(cudaStreamSynchronize(stream));
   return true;
 }
@@ -203,101 +230,98 @@ void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
 }
 
 void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
-  if (!ensure_fill_scratch(0)) return;
-  if (warp_fill_ && !ensure_wscratch()) return;
+  const bool warp = warp_fill_ != 0;
+  const bool team = warp && team_fill_ != 0;
+  if (warp && !ensure_wscratch()) return;
+  if (team && !ensure_tscratch()) return;
+  if (!team && !ensure_fill_scratch(0)) return;
   // the tables are shared: start after the previous fill, on any stream (a
   // graph being captured is ordered at its launch instead)
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   check(cudaStreamIsCapturing(st, &cap));
   const bool capturing = cap != cudaStreamCaptureStatusNone;
   if (!capturing) fill_after(st);
-  FillScratch s = fs_[0];
-  // largest points first; the head of the list goes to the large tables
+  // largest points first; in the CTA fill the head of the list goes to its
+  // large tables
   char* ob = (char*)order_.need(sizeof(int32_t) * np + 1024);
   unsigned* order_meta = (unsigned*)ob;
   int32_t* order_list = (int32_t*)(ob + 1024);
   launch_order(R.points, (int)np, order_list, order_meta, big_units_, st);
-  s.nbig = order_meta + 1;
-  s.dump = R.dump;
-  s.dump_count = R.dump_count;
-  s.dump_cap = R.dump_cap;
-  unsigned long long* prof = nullptr;
-  if (profiling) {
-    prof = (unsigned long long*)prof_.need(8 * sizeof(unsigned long long));
-    cudaMemsetAsync(prof, 0, 8 * sizeof(unsigned long long), st);
-    s.prof = prof;
+  // points left over by one stage (status bit 4) are listed for the next;
+  // the launches read their point count on the device, so no host round trip
+  // is needed (a launch with an empty list exits at once)
+  char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
+  int32_t* list = (int32_t*)(rb + 64);
+  unsigned* count = (unsigned*)rb;
+  cudaEvent_t pe[3] = {nullptr, nullptr, nullptr};
+  if (profiling && warp) {
+    for (auto& e : pe) cudaEventCreate(&e);
+    cudaEventRecord(pe[0], st);
   }
-  if (heartbeat_words_ == 0 && getenv("TL_HEARTBEAT")) {
-    heartbeat_words_ = 1 << 16;
-    cudaHostAlloc((void**)&heartbeat_host_, heartbeat_words_ * 8, cudaHostAllocMapped);
-    cudaHostGetDevicePointer((void**)&heartbeat_dev_, heartbeat_host_, 0);
-  }
-  s.heartbeat = heartbeat_dev_;
-  if (warp_fill_) {
-    // one warp per point for every point up to wfill_thr_ predicted blocks;
-    // the larger ones, and those whose warp table fills up, come back with
-    // status bit 4 and go to the CTA fill below (all its levels)
+  if (warp) {
+    // one warp per point for every point up to wfill_thr_ predicted blocks
     WScratch w = ws_;
     w.wthr = wfill_thr_;
     w.dump = R.dump;
     w.dump_count = R.dump_count;
     w.dump_cap = R.dump_cap;
+    unsigned long long* wprof = nullptr;
+    if (profiling) {
+      wprof = (unsigned long long*)wprof_.need(8 * sizeof(unsigned long long));
+      cudaMemsetAsync(wprof, 0, 8 * sizeof(unsigned long long), st);
+      w.prof = wprof;
+    }
     launch_wfill(R.points, (int)np, d_lenses, R.seeds, R.out, w, mode, st, order_list,
                  order_meta);
+    if (profiling) {
+      cudaEventRecord(pe[1], st);
+      unsigned long long h[8];
+      cudaMemcpyAsync(h, wprof, sizeof(h), cudaMemcpyDeviceToHost, st);
+      cudaStreamSynchronize(st);
+      fprintf(stderr,
+              "[tl wprof] points %llu  visits %llu  first visits %llu  super-tiles %llu  "
+              "probe rounds %llu  inserted %llu  whole %llu  ray-by-ray weights %llu\n",
+              h[7], h[0], h[1], h[2], h[3], h[4], h[5], h[6]);
+    }
+    if (team) {
+      // the larger points (and those whose warp table filled up): 8 warps each
+      WScratch t = ts_;
+      t.dump = R.dump;
+      t.dump_count = R.dump_count;
+      t.dump_cap = R.dump_cap;
+      launch_collect_overflow(R.out, (int)np, list, count, st);
+      launch_tfill(R.points, (int)np, d_lenses, R.seeds, R.out, t, mode, st, list, count);
+    }
   } else {
+    FillScratch s = fs_[0];
+    s.nbig = order_meta + 1;
+    s.dump = R.dump;
+    s.dump_count = R.dump_count;
+    s.dump_cap = R.dump_cap;
+    unsigned long long* prof = nullptr;
+    if (profiling) {
+      prof = (unsigned long long*)prof_.need(8 * sizeof(unsigned long long));
+      cudaMemsetAsync(prof, 0, 8 * sizeof(unsigned long long), st);
+      s.prof = prof;
+    }
     launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st, order_list,
                 order_meta);
+    if (profiling) {
+      unsigned long long h[8];
+      cudaMemcpyAsync(h, prof, sizeof(h), cudaMemcpyDeviceToHost, st);
+      cudaStreamSynchronize(st);
+      fprintf(stderr,
+              "[tl prof] tiles %llu  cyc/tile %.0f  idle polls %llu  work-loop cyc %llu  "
+              "supertiles %llu  cyc/supertile %.0f  eval cyc/tile %.0f  push cyc/tile %.0f\n",
+              h[0], h[0] ? (double)h[1] / h[0] : 0.0, h[2], h[3], h[4],
+              h[4] ? (double)h[5] / h[4] : 0.0, h[0] ? (double)h[6] / h[0] : 0.0,
+              h[0] ? (double)h[7] / h[0] : 0.0);
+    }
   }
-  if (heartbeat_host_) {
-    // a side thread reports the warps' phases while the stream is busy; the
-    // caller keeps blocking as usual
-    const int nw = s.ctas * (threads_ / 32);
-    unsigned long long* hb = heartbeat_host_;
-    std::atomic<bool> done(false);
-    std::thread watch([hb, nw, &done]() {
-      for (int it = 1; !done.load() && it < 600; it++) {
-        for (int k = 0; k < 20 && !done.load(); k++) usleep(100000);
-        if (done.load()) break;
-        int hist[16] = {0};
-        for (int w = 0; w < nw; w++) hist[(hb[w] >> 56) & 15]++;
-        fprintf(stderr, "[tl hb] %ds phases:", 2 * it);
-        for (int k = 0; k < 9; k++) fprintf(stderr, " %d:%d", k, hist[k]);
-        fprintf(stderr, "\n");
-        int shown = 0;
-        for (int w = 0; w < nw && shown < 16; w++) {
-          const unsigned long long v = hb[w];
-          const int ph = (int)((v >> 56) & 15);
-          if (ph != 0 && ph != 8) {
-            fprintf(stderr, "   warp %d cta %d phase %d point %llu step %llu\n", w, w / 8, ph,
-                    (v >> 24) & 0xffffffffull, v & 0xffffffull);
-            shown++;
-          }
-        }
-      }
-    });
-    cudaStreamSynchronize(st);
-    done.store(true);
-    watch.join();
-  }
-  if (profiling) {
-    unsigned long long h[8];
-    cudaMemcpyAsync(h, prof, sizeof(h), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    fprintf(stderr,
-            "[tl prof] tiles %llu  cyc/tile %.0f  idle polls %llu  work-loop cyc %llu  "
-            "supertiles %llu  cyc/supertile %.0f  eval cyc/tile %.0f  push cyc/tile %.0f\n",
-            h[0], h[0] ? (double)h[1] / h[0] : 0.0, h[2], h[3], h[4],
-            h[4] ? (double)h[5] / h[4] : 0.0, h[0] ? (double)h[6] / h[0] : 0.0,
-            h[0] ? (double)h[7] / h[0] : 0.0);
-  }
-  // points whose tile table overflowed run again with larger tables; the
-  // retry launches read their point count on the device, so no host round
-  // trip is needed (a retry with an empty list exits at once)
-  char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
-  int32_t* list = (int32_t*)(rb + 64);
-  unsigned* count = (unsigned*)rb;
-  for (int level = warp_fill_ ? 0 : 1; level < kFillLevels && level < levels_ + warp_fill_;
-       level++) {
+  if (profiling && warp) cudaEventRecord(pe[2], st);
+  // points whose table overflowed run again with larger tables (CTA fill;
+  // level 0 only when neither the team fill nor the CTA fill has run)
+  for (int level = warp && !team ? 0 : 1; level < kFillLevels && level < levels_; level++) {
     if (!ensure_fill_scratch(level)) break;
     FillScratch sl = fs_[level];
     sl.nbig = nullptr;   // a retry list is not size-ordered: every CTA takes from it
@@ -306,6 +330,20 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     sl.dump_cap = R.dump_cap;
     launch_collect_overflow(R.out, (int)np, list, count, st);
     launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, sl, mode, threads_, st, list, count);
+  }
+  if (profiling && warp) {
+    cudaEvent_t e3;
+    cudaEventCreate(&e3);
+    cudaEventRecord(e3, st);
+    cudaEventSynchronize(e3);
+    float a = 0.f, b = 0.f, c = 0.f;
+    cudaEventElapsedTime(&a, pe[0], pe[1]);
+    cudaEventElapsedTime(&b, pe[1], pe[2]);
+    cudaEventElapsedTime(&c, pe[2], e3);
+    fprintf(stderr, "[tl wprof] warp fill %.1f ms, team fill %.1f ms, CTA-fill levels %.1f ms\n",
+            a, b, c);
+    for (auto& e : pe) cudaEventDestroy(e);
+    cudaEventDestroy(e3);
   }
   if (!capturing) fill_mark(st);
   check(cudaGetLastError());

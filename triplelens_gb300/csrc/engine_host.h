@@ -103,8 +103,17 @@ class Engine {
   // the CTA fill the rest (TL_FILL_KERNEL=cta: the CTA fill alone)
   int warp_fill_ = 1;
   unsigned wfill_thr_ = 7000;
+  int want_wfill_warps_ = 0;
+  int wfill_cap_log2_ = 14;
+  // the team fill (8 warps per point) takes the points the warp fill leaves
+  bool ensure_tscratch();
+  void* tfill_base_ = nullptr;
+  WScratch ts_{};
+  int team_fill_ = 1;
+  int want_teams_ = 0;
+  static constexpr int kTeamCapLog2 = 15;   // slots per team warp's table
   RunBufs run_;
-  DevBuf retry_, prof_, order_;
+  DevBuf retry_, prof_, order_, wprof_;
   cudaEvent_t fill_done_ = nullptr;   // the last fill launched
   int want_big_ctas_ = -1;   // -1: 64 when there are >= 256 CTAs, else a quarter
   unsigned big_units_ = 0;

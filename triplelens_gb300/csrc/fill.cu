@@ -752,6 +752,70 @@ __device__ __noinline__ float weight_again(const Ctx& c, const SuperTile& st, bo
   return ld_weight_f(c, r2);
 }
 
+// Weights of the rays of f (lane r: row r's mask) in block (bx, by) of
+// super-tile st, one lane per column: the split map once per filled ray,
+// the same formula and summation order as weight_again over the rows.
+template <int K>
+__device__ __forceinline__ float partial_weights(const Ctx& c, const SuperTile& st, int bx,
+                                                 int by, int lane, uint32_t f, unsigned* nre) {
+  const float hf = c.hf;
+  const int64_t nx = (int64_t)bx * 32 + lane;
+  const float dx = hf * (float)(int)(nx - st.nxc);
+  const float bxo = st.d0x + dx;
+  const int dy0 = (int)((int64_t)by * 32 - st.nyc);
+  float acc = 0.f;
+  unsigned re = 0;
+#pragma unroll 1
+  for (int r = 0; r < 32; r++) {
+    const uint32_t nwr = __shfl_sync(0xffffffffu, f, r);
+    if (nwr == 0u) continue;   // the same in every lane
+    const bool on = (nwr >> lane) & 1u;
+    const float dy = hf * (float)(dy0 + r);
+    const float w = ld_weight_f(c, split_r2<K>(c, st, dx, bxo, dy));
+    acc += on ? w : 0.f;
+    re += on ? 1u : 0u;
+  }
+  *nre = re;
+  return acc;
+}
+
+// weights of the rays of f in a 32 x 32 block (whole warp): inline for the
+// split map, ray by ray in FP64 otherwise (as weight_again)
+__device__ __forceinline__ float block_weights(const Ctx& c, const SuperTile& st, bool split,
+                                               int bx, int by, int lane, uint32_t f,
+                                               unsigned* nre) {
+  if (split && st.mode == kModeTaylor)
+    return st.K <= 2 ? partial_weights<2>(c, st, bx, by, lane, f, nre)
+                     : partial_weights<4>(c, st, bx, by, lane, f, nre);
+  if (split && st.mode == kModeExact32) return partial_weights<0>(c, st, bx, by, lane, f, nre);
+  float acc = 0.f;
+  unsigned re = 0;
+  const int64_t nx = (int64_t)bx * 32 + lane;
+#pragma unroll 1
+  for (int r = 0; r < 32; r++) {
+    const uint32_t nwr = __shfl_sync(0xffffffffu, f, r);
+    if ((nwr >> lane) & 1u) {
+      acc += weight_again(c, st, split, nx, (int64_t)by * 32 + r);
+      re++;
+    }
+  }
+  *nre = re;
+  return acc;
+}
+
+// Whole warp: true when hp (lane r: row r's mask) is 4-connected by a simple
+// test: one run per row, its non-empty rows consecutive, each row's run
+// overlapping the next row's.  A fill entering such a set anywhere fills
+// all of it.
+__device__ __forceinline__ bool simple_region(uint32_t hp, int lane) {
+  const bool one_run = (hp & (hp + (hp & (0u - hp)))) == 0u;
+  const uint32_t nxt = __shfl_down_sync(0xffffffffu, hp, 1);
+  const bool link = lane == 31 || hp == 0u || nxt == 0u || (hp & nxt) != 0u;
+  const uint32_t nz = __ballot_sync(0xffffffffu, hp != 0u);
+  const bool rows = (nz & (nz + (nz & (0u - nz)))) == 0u;
+  return __all_sync(0xffffffffu, one_run && link) && rows;
+}
+
 // per-warp cache of the last super-tile used
 struct WarpST {
   uint64_t key;
@@ -849,7 +913,9 @@ __device__ void process_block(Shared& S, const Table& T, int slot, int lane, War
       // every iteration that changes anything fills at least one more run,
       // so 32 rows x 16 runs bounds it
       if (lane == 0) beat(S.hb, 4, S.point, 0);
-      for (int it = 0; it < 1024; it++) {
+      const bool whole = simple_region(hp, lane);   // filled whole by any entry
+      if (whole) f = hp;
+      for (int it = 0; it < 1024 && !whole; it++) {
         if ((it & 63) == 63) {
           unsigned late = 0;
           if (lane == 0) late = overdue(S, 6);
@@ -883,12 +949,16 @@ __device__ void process_block(Shared& S, const Table& T, int slot, int lane, War
         unsigned re = 0;
         const int64_t nx = (int64_t)bx * 32 + lane;
         if (c.split) warp_supertile<BH>(S, T, bx, by, lane, wst);
+        if (BH == 32) {
+          acc = block_weights(c, wst.st, c.split && wst.valid, bx, by, lane, f, &re);
+        } else {
 #pragma unroll 1
-        for (int r = 0; r < BH; r++) {
-          const uint32_t nwr = __shfl_sync(0xffffffffu, f, r);
-          if ((nwr >> lane) & 1u) {
-            acc += weight_again(c, wst.st, c.split && wst.valid, nx, (int64_t)by * BH + r);
-            re++;
+          for (int r = 0; r < BH; r++) {
+            const uint32_t nwr = __shfl_sync(0xffffffffu, f, r);
+            if ((nwr >> lane) & 1u) {
+              acc += weight_again(c, wst.st, c.split && wst.valid, nx, (int64_t)by * BH + r);
+              re++;
+            }
           }
         }
         local_eval += warp_sum_u(re);
@@ -1189,8 +1259,8 @@ fill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int
 // Warp fill.  One warp fills one point alone, points taken from the
 // size-ordered list (largest first).  The point's blocks of 32 x 32 rays sit
 // in the warp's own open-addressing table in HBM; the work stack (spilling
-// into HBM past kWStack entries), the queued bitmap, the last super-tile
-// expansions and the seed pixels in shared memory.  Each visit of a block
+// into HBM past kWStack entries), the last super-tile expansions and the
+// seed pixels in shared memory; a slot's header says whether it is queued.  Each visit of a block
 // does what process_block does (classification, closure, weights, edge
 // test), and the warp is the only writer of its table: no atomics on the
 // table and no waits on other warps.  A block's four neighbours are looked
@@ -1201,26 +1271,21 @@ namespace {
 constexpr int kWThreads = 128;                   // 4 warps per CTA
 constexpr int kWWarps = kWThreads / 32;
 constexpr int kWOcc = 8;                         // resident CTAs per SM (32 warps)
-constexpr int kWCap = 1 << kWCapLog2;
-constexpr uint32_t kWMask = (uint32_t)kWCap - 1u;
 constexpr int kWStack = 512;                     // work-stack entries in shared memory
 constexpr int kWStCache = 8;                     // super-tile expansions kept per warp
-constexpr unsigned kWUsable = kWCap / 4 * 3;     // table load limit (blocks per point)
-constexpr unsigned kWPopLimit = 16u * kWCap;     // bound on block visits per point
-constexpr int kWProbeIters = 4 * (kWCap / 8 + 2);
 constexpr unsigned kFull = 0xffffffffu;
 // header words
 constexpr int kHEb = 0, kHEt = 1, kHEl = 2, kHEr = 3;   // entry masks: bottom/top row, left/right column
 constexpr int kHFb = 4, kHFt = 5, kHFl = 6, kHFr = 7;   // filled border: row 0, row 31, column 0, column 31
 constexpr int kHState = 8, kHBx = 9, kHBy = 10;
-constexpr uint32_t kWCls = 1u, kWSeed = 2u;             // state: H and F valid; holds a seed pixel
+// state: H and F valid; holds a seed pixel; on the work stack
+constexpr uint32_t kWCls = 1u, kWSeed = 2u, kWQueued = 4u;
 
 struct WarpSh {
   Ctx c;
   SuperTile st[kWStCache];
   uint64_t sttag[kWStCache];
   uint32_t stack[kWStack];
-  uint32_t queued[kWCap / 32];
   int32_t seedx[kMaxSeeds], seedy[kMaxSeeds];
   unsigned top, used, nseed;
 };
@@ -1231,21 +1296,23 @@ struct WTable {
   uint32_t* body;
   uint32_t* used;
   uint32_t* spill;
+  uint32_t mask;      // slots - 1
+  unsigned usable;    // table load limit (blocks per point): 3/4 of the slots
 };
 
 struct WAcc {
   unsigned long long count, eval, fp64;
   long long fx;       // weight sum, units of 2^-16 (lane 0's value is used)
   unsigned edge;
+  unsigned prof[8];   // optional counters (WScratch::prof), lane 0's values
 };
 
-// one lane: queue `slot` unless it is queued already
-__device__ __forceinline__ void w_queue(WarpSh& W, const WTable& T, uint32_t slot) {
-  const uint32_t bit = 1u << (slot & 31u);
-  if (atomicOr(&W.queued[slot >> 5], bit) & bit) return;
+// one lane: put `slot` on the work stack (its header's state says queued
+// from now until its visit writes the header back)
+__device__ __forceinline__ void w_push_stack(WarpSh& W, const WTable& T, uint32_t slot) {
   const unsigned pos = atomicAdd(&W.top, 1u);
   if (pos < (unsigned)kWStack) W.stack[pos] = slot;
-  else __stcg(&T.spill[pos], slot);   // pos < number of queued slots <= kWCap
+  else __stcg(&T.spill[pos], slot);   // pos < number of queued slots <= slots
 }
 
 // Whole warp.  The 8 lanes of group g = lane / 8 look up block (bx, by) when
@@ -1254,24 +1321,26 @@ __device__ __forceinline__ void w_queue(WarpSh& W, const WTable& T, uint32_t slo
 // now.  Groups that pick the same free slot in one round: the lower group
 // takes it, the other reads its window again.
 __device__ __noinline__ int w_find4(const WTable& T, bool act, int bx, int by, int lane,
-                                    bool* ins) {
+                                    bool* ins, unsigned* rounds) {
   const int g = lane >> 3, j = lane & 7;
   const uint64_t key = tile_key(bx, by);
-  const uint32_t h0 = hash_key(key) & kWMask;
+  const uint32_t h0 = hash_key(key) & T.mask;
   int slot = -1;
   bool done = !act, inserted = false;
   uint32_t r = 0;
-  for (int it = 0; it < kWProbeIters; it++) {
+  const int iters = 4 * (int)(T.mask / 8u + 2u);
+  for (int it = 0; it < iters; it++) {
     const bool live = !done;
     if (!__any_sync(kFull, live)) break;
+    ++*rounds;
     const uint32_t base = h0 + r * 8u;
     uint64_t k = 0;
-    if (live) k = ldcg64(&T.keys[(base + (uint32_t)j) & kWMask]);
+    if (live) k = ldcg64(&T.keys[(base + (uint32_t)j) & T.mask]);
     const uint32_t mm = __ballot_sync(kFull, live && k == key);
     const uint32_t me = __ballot_sync(kFull, live && k == kEmptyKey);
     const uint32_t gm = (mm >> (8 * g)) & 0xffu, ge = (me >> (8 * g)) & 0xffu;
     uint32_t want = kFull;
-    if (live && gm == 0u && ge != 0u) want = (base + (uint32_t)(__ffs(ge) - 1)) & kWMask;
+    if (live && gm == 0u && ge != 0u) want = (base + (uint32_t)(__ffs(ge) - 1)) & T.mask;
     const uint32_t w0 = __shfl_sync(kFull, want, 0);
     const uint32_t w1 = __shfl_sync(kFull, want, 8);
     const uint32_t w2 = __shfl_sync(kFull, want, 16);
@@ -1280,7 +1349,7 @@ __device__ __noinline__ int w_find4(const WTable& T, bool act, int bx, int by, i
     bool take = false;
     if (live) {
       if (gm != 0u) {
-        slot = (int)((base + (uint32_t)(__ffs(gm) - 1)) & kWMask);
+        slot = (int)((base + (uint32_t)(__ffs(gm) - 1)) & T.mask);
         done = true;
       } else if (want != kFull) {
         if (!lose) {
@@ -1291,7 +1360,7 @@ __device__ __noinline__ int w_find4(const WTable& T, bool act, int bx, int by, i
         }
       } else {
         r++;
-        if (r > kWMask / 8u) done = true;   // every window holds other keys: no slot
+        if (r > T.mask / 8u) done = true;   // every window holds other keys: no slot
       }
     }
     if (take && j == 0) __stcg((unsigned long long*)&T.keys[slot], (unsigned long long)key);
@@ -1311,18 +1380,19 @@ __device__ __forceinline__ void w_init_slot(WarpSh& W, const WTable& T, int slot
     __stcg(&h[q], q == kHBx ? (uint32_t)bx : (q == kHBy ? (uint32_t)by : 0u));
   if (j == 0) {
     const unsigned u = atomicAdd(&W.used, 1u);
-    if (u < (unsigned)kWCap) __stcg(&T.used[u], (uint32_t)slot);
+    if (u <= T.mask) __stcg(&T.used[u], (uint32_t)slot);
   }
 }
 
 // whole warp: cache index of the expansion of the super-tile holding block
 // (bx, by), computed on a miss
-__device__ __noinline__ int w_supertile(WarpSh& W, int bx, int by, int lane) {
+__device__ __noinline__ int w_supertile(WarpSh& W, int bx, int by, int lane, unsigned* misses) {
   const int sh = W.c.slog2 - 5;
   const int sxi = bx >> sh, syi = by >> sh;
   const uint64_t key = tile_key(sxi, syi);
   const int idx = (int)(hash_key(key) & (uint32_t)(kWStCache - 1));
   if (W.sttag[idx] != key) {
+    ++*misses;
     SuperTile v;
     supertile_values(W.c, sxi, syi, lane, &v);
     __syncwarp();
@@ -1335,9 +1405,56 @@ __device__ __noinline__ int w_supertile(WarpSh& W, int bx, int by, int lane) {
   return idx;
 }
 
-// whole warp: one visit of the block in `slot`
+// A team of kTeamWarps warps filling one point together (tfill_kernel):
+// each warp owns the blocks of its share of the super-tiles; entries into a
+// block of another share go to that warp's inbox as messages (block, side,
+// bits), read at the start of the next round.
+constexpr int kTeamWarps = 8;
+struct WTeam {
+  uint4* inbox;            // this team's inboxes: [2 buffers][kTeamWarps][cap]
+  unsigned* inbox_n;       // shared counters [2][kTeamWarps]
+  unsigned* abort_;        // shared: status bits that end the point
+  unsigned cap;            // messages per inbox
+  int me;                  // this warp's share
+  int post;                // buffer taking this round's messages
+  int sh;                  // log2 of the super-tile edge in blocks
+};
+
+__device__ __forceinline__ int team_owner(int bx, int by, int sh) {
+  return (int)(hash_key(tile_key(bx >> sh, by >> sh)) & (uint32_t)(kTeamWarps - 1));
+}
+
+// entry and filled-border words of a block side (side 0: bottom row, from
+// the block below; 1: top row; 2: column 31; 3: column 0)
+__device__ __forceinline__ void side_words(int side, int* ew, int* fw) {
+  *ew = side == 0 ? kHEb : (side == 1 ? kHEt : (side == 2 ? kHEr : kHEl));
+  *fw = side == 0 ? kHFb : (side == 1 ? kHFt : (side == 2 ? kHFr : kHFl));
+}
+
+// one lane: entry bits into slot s (inserted now: header zero), less what it
+// has filled; queued if new bits arrived and it is not queued yet
+__device__ __forceinline__ void w_enter(WarpSh& W, const WTable& T, int s, bool ins, int side,
+                                        uint32_t bits) {
+  int ew, fw;
+  side_words(side, &ew, &fw);
+  uint32_t* nh = T.hdr + (size_t)s * kWHdrWords;
+  const uint32_t filled = ins ? 0u : ldcg32(&nh[fw]);
+  const uint32_t old = ins ? 0u : ldcg32(&nh[ew]);
+  const uint32_t nst = ins ? 0u : ldcg32(&nh[kHState]);
+  const uint32_t nb = bits & ~filled;
+  if (nb) {
+    __stcg(&nh[ew], old | nb);
+    if (!(nst & kWQueued)) {
+      __stcg(&nh[kHState], nst | kWQueued);
+      w_push_stack(W, T, (uint32_t)s);
+    }
+  }
+}
+
+// whole warp: one visit of the block in `slot`; tm: the warp's team (null
+// for the warp fill, where every block is the warp's own)
 __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, int lane,
-                                     WAcc& A) {
+                                     WAcc& A, const WTeam* tm) {
   const Ctx& c = W.c;
   uint32_t* hdr = T.hdr + (size_t)slot * kWHdrWords;
   uint32_t* body = T.body + (size_t)slot * 64;
@@ -1365,7 +1482,7 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
   int sti = -1;
   if (!cls) {
     unsigned nr = 0, n64 = 0;
-    if (c.split) sti = w_supertile(W, bx, by, lane);
+    if (c.split) sti = w_supertile(W, bx, by, lane, &A.prof[2]);
     if (sti >= 0 && W.st[sti].mode != kModeFp64) {
       const SuperTile stc = W.st[sti];   // by value: the coefficients stay in registers
       const int K = stc.mode == kModeTaylor ? stc.K : 0;
@@ -1378,15 +1495,23 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
     A.eval += warp_sum_u(nr);
     A.fp64 += warp_sum_u(n64);
     fresh = true;
+    A.prof[1]++;
   }
+  A.prof[0]++;
   const uint32_t hp = h_row & ~f_cur;   // accepted, not yet filled
   uint32_t f = e_row & hp;
   uint32_t f_new = f_cur;
   const bool any = __ballot_sync(kFull, f != 0u) != 0u;
   uint32_t top = 0, bot = 0, lcol = 0, rcol = 0;
   if (any) {
-    // closure inside the block (as process_block)
-    for (int it = 0; it < 1024; it++) {
+    // closure inside the block (as process_block); a simply connected hp is
+    // filled whole by any entry
+    const bool whole = simple_region(hp, lane);
+    if (whole) {
+      f = hp;
+      A.prof[5]++;
+    }
+    for (int it = 0; it < 1024 && !whole; it++) {
       uint32_t below = __shfl_up_sync(kFull, f, 1);
       uint32_t above = __shfl_down_sync(kFull, f, 1);
       if (lane == 0) below = 0u;
@@ -1404,19 +1529,11 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
     if (all) {
       acc = wall;
     } else {
-      acc = 0.f;
       unsigned re = 0;
-      if (c.split && sti < 0) sti = w_supertile(W, bx, by, lane);
+      A.prof[6]++;
+      if (c.split && sti < 0) sti = w_supertile(W, bx, by, lane, &A.prof[2]);
       const SuperTile stw = sti >= 0 ? W.st[sti] : SuperTile{};
-      const int64_t nx = (int64_t)bx * 32 + lane;
-#pragma unroll 1
-      for (int r = 0; r < 32; r++) {
-        const uint32_t nwr = __shfl_sync(kFull, f, r);
-        if ((nwr >> lane) & 1u) {
-          acc += weight_again(c, stw, c.split && sti >= 0, nx, (int64_t)by * 32 + r);
-          re++;
-        }
-      }
+      acc = block_weights(c, stw, c.split && sti >= 0, bx, by, lane, f, &re);
       A.eval += warp_sum_u(re);
     }
     A.count += warp_sum_u(__popc(f));
@@ -1447,7 +1564,7 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
     else if (lane == kHFt) v = fr31;
     else if (lane == kHFl) v = flb;
     else if (lane == kHFr) v = frb;
-    else if (lane == kHState) v = state | kWCls;
+    else if (lane == kHState) v = (state | kWCls) & ~kWQueued;
     __stcg(&hdr[lane], v);
   }
   __syncwarp();
@@ -1455,28 +1572,154 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
   // neighbours: group 0 the block above (its bottom row), 1 below (its top
   // row), 2 left (its column 31), 3 right (its column 0)
   const int g = lane >> 3, j = lane & 7;
-  int nbx = bx, nby = by, ew, fw;
+  int nbx = bx, nby = by;
   uint32_t bits;
-  if (g == 0) { nby = by + 1; bits = top; ew = kHEb; fw = kHFb; }
-  else if (g == 1) { nby = by - 1; bits = bot; ew = kHEt; fw = kHFt; }
-  else if (g == 2) { nbx = bx - 1; bits = lcol; ew = kHEr; fw = kHFr; }
-  else { nbx = bx + 1; bits = rcol; ew = kHEl; fw = kHFl; }
-  const bool act = bits != 0u && nbx >= 0 && nby >= 0 && nbx <= c.txmax && nby <= c.tymax;
+  if (g == 0) { nby = by + 1; bits = top; }
+  else if (g == 1) { nby = by - 1; bits = bot; }
+  else if (g == 2) { nbx = bx - 1; bits = lcol; }
+  else { nbx = bx + 1; bits = rcol; }
+  const bool inplane = bits != 0u && nbx >= 0 && nby >= 0 && nbx <= c.txmax && nby <= c.tymax;
+  int owner = 0;
+  if (tm && inplane) owner = team_owner(nbx, nby, tm->sh);
+  const bool remote = tm && inplane && owner != tm->me;
+  const bool act = inplane && !remote;
   bool ins = false;
-  const int s = w_find4(T, act, nbx, nby, lane, &ins);
+  const int s = w_find4(T, act, nbx, nby, lane, &ins, &A.prof[3]);
   if (s >= 0 && ins) w_init_slot(W, T, s, nbx, nby, lane);
+  A.prof[4] += (unsigned)__popc(__ballot_sync(kFull, s >= 0 && ins && j == 0));
   __syncwarp();
-  if (s >= 0 && j == 0) {
-    uint32_t* nh = T.hdr + (size_t)s * kWHdrWords;
-    const uint32_t filled = ins ? 0u : ldcg32(&nh[fw]);
-    const uint32_t old = ins ? 0u : ldcg32(&nh[ew]);
-    const uint32_t nb = bits & ~filled;
-    if (nb) {
-      __stcg(&nh[ew], old | nb);
-      w_queue(W, T, (uint32_t)s);
-    }
+  if (s >= 0 && j == 0) w_enter(W, T, s, ins, g, bits);
+  if (remote && j == 0) {
+    const unsigned k = atomicAdd(&tm->inbox_n[tm->post * kTeamWarps + owner], 1u);
+    if (k < tm->cap)
+      tm->inbox[((size_t)tm->post * kTeamWarps + owner) * tm->cap + k] =
+          make_uint4((uint32_t)nbx, (uint32_t)nby, (uint32_t)g, bits);
+    else
+      atomicOr(tm->abort_, (unsigned)kStTableFull);
   }
   __syncwarp();
+}
+
+// lane 0 sets the warp's point context (the CTA fill's Ctx, 32-row blocks);
+// whole warp clears the super-tile cache
+__device__ __forceinline__ void w_context(WarpSh& W, const PointIn& pi, const DevLens* lenses,
+                                          int split_mode, int lane) {
+  if (lane == 0) {
+    const DevLens& D = lenses[pi.lens];
+    Ctx& c = W.c;
+    c.sx = pi.sx;
+    c.sy = pi.sy;
+    c.cx0 = D.g.corner_x;
+    c.cy0 = D.g.corner_y;
+    c.h = D.g.h;
+    c.n = D.g.n;
+    c.rho = D.rho;
+    c.rho2 = D.rho2;
+    c.ld_a = D.ld_a;
+    c.ld_b = D.ld_b;
+    c.m1 = D.L.m1;
+    c.m2 = D.L.m2;
+    c.m3 = D.L.m3;
+    c.z2x = D.L.z2.re;
+    c.z3x = D.L.z3.re;
+    c.z3y = D.L.z3.im;
+    c.binary = D.ray_binary;
+    c.txmax = (int)((c.n - 1) >> 5);
+    c.tymax = (int)((c.n - 1) >> 5);
+    c.split = split_mode;
+    // super-tile edge as the CTA fill: 2^9 pixels, down to 2^7 as h grows
+    int sl = 9;
+    while (sl > 7 && c.h * (double)(1 << sl) > 1.5e-3) sl--;
+    c.slog2 = sl;
+    c.hf = (float)c.h;
+    c.rho2f = (float)c.rho2;
+    c.inv_rho2f = (float)(1.0 / c.rho2);
+    c.ldaf = (float)c.ld_a;
+    c.ldbf = (float)c.ld_b;
+    W.top = 0;
+    W.used = 0;
+    W.nseed = 0;
+  }
+  if (lane < kWStCache) W.sttag[lane] = kEmptyKey;
+  __syncwarp();
+}
+
+// whole warp: the point's seed pixels (lcirs.cc:171-174; seed rows must
+// satisfy 0 < ny < N, 386-391) into W.seedx/seedy; returns kStEdge when a
+// seed lies outside columns 1..N-1
+__device__ __forceinline__ uint32_t w_load_seeds(WarpSh& W, int p, const int32_t* seeds,
+                                                 const PointOut* out, int lane) {
+  const int64_t n = W.c.n;
+  uint32_t status = 0;
+  const unsigned ns = min(out[p].nseeds, (unsigned)kMaxSeeds);
+  for (unsigned k0 = 0; k0 < ns; k0 += 32) {
+    const unsigned k = k0 + (unsigned)lane;
+    int32_t px = 0, py = 0;
+    bool ok = false, edge = false;
+    if (k < ns) {
+      px = seeds[((size_t)p * kMaxSeeds + k) * 2];
+      py = seeds[((size_t)p * kMaxSeeds + k) * 2 + 1];
+      if (py > 0 && (int64_t)py < n) {
+        if (px < 1 || (int64_t)px > n - 1) edge = true;
+        else ok = true;
+      }
+    }
+    if (__any_sync(kFull, edge)) status |= kStEdge;
+    const uint32_t okm = __ballot_sync(kFull, ok);
+    if (ok) {
+      const unsigned pos = W.nseed + (unsigned)__popc(okm & ((1u << lane) - 1u));
+      W.seedx[pos] = px;
+      W.seedy[pos] = py;
+    }
+    __syncwarp();
+    if (lane == 0) W.nseed += (unsigned)__popc(okm);
+    __syncwarp();
+  }
+  return status;
+}
+
+// whole warp: the amoeba export (32 x 8 tiles of F, as the CTA fill) of
+// the point's blocks when `complete`, and the clearing of the slots used
+__device__ __forceinline__ void w_finish(const WTable& T, const WScratch& sc, int p,
+                                         unsigned nused, bool complete, int lane) {
+  for (unsigned u = (unsigned)lane; u < nused; u += 32) {
+    const uint32_t slot = ldcg32(&T.used[u]);
+    if (sc.dump && complete) {
+      const uint32_t* h = T.hdr + (size_t)slot * kWHdrWords;
+      if (ldcg32(&h[kHState]) & kWCls) {
+        const uint32_t* b = T.body + (size_t)slot * 64;
+        const uint32_t bxk = ldcg32(&h[kHBx]), byk = ldcg32(&h[kHBy]);
+        for (int t8 = 0; t8 < 4; t8++) {
+          uint32_t fm[8], a8 = 0;
+          for (int r = 0; r < 8; r++) a8 |= (fm[r] = ldcg32(&b[32 + 8 * t8 + r]));
+          if (!a8) continue;
+          const unsigned d = atomicAdd(sc.dump_count, 1u);
+          if (d < sc.dump_cap) {
+            uint32_t* o = sc.dump + (size_t)d * kDumpWords;
+            o[0] = (uint32_t)p;
+            o[1] = bxk;
+            o[2] = byk * 4u + (uint32_t)t8;
+            for (int r = 0; r < 8; r++) o[3 + r] = fm[r];
+          }
+        }
+      }
+    }
+    __stcg((unsigned long long*)&T.keys[slot], (unsigned long long)kEmptyKey);
+  }
+}
+
+// the warp's table inside a WScratch
+__device__ __forceinline__ WTable w_table(const WScratch& sc, size_t gw) {
+  WTable T;
+  const size_t slots = (size_t)1 << sc.cap_log2;
+  T.keys = sc.keys + gw * slots;
+  T.hdr = sc.hdr + gw * slots * kWHdrWords;
+  T.body = sc.body + gw * slots * 64;
+  T.used = sc.used + gw * slots;
+  T.spill = sc.spill + gw * slots;
+  T.mask = (uint32_t)(slots - 1);
+  T.usable = (unsigned)(slots / 4 * 3);
+  return T;
 }
 
 }  // namespace
@@ -1491,15 +1734,10 @@ wfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
   WarpSh& W = wsh[threadIdx.x >> 5];
   const size_t gw = (size_t)blockIdx.x * kWWarps + (threadIdx.x >> 5);
   if (gw >= (size_t)sc.warps) return;   // whole warps; the kernel has no block barrier
-  WTable T;
-  T.keys = sc.keys + (gw << kWCapLog2);
-  T.hdr = sc.hdr + (gw << kWCapLog2) * kWHdrWords;
-  T.body = sc.body + (gw << kWCapLog2) * 64;
-  T.used = sc.used + (gw << kWCapLog2);
-  T.spill = sc.spill + (gw << kWCapLog2);
+  const WTable T = w_table(sc, gw);
+  const size_t slots = (size_t)T.mask + 1;
+  const unsigned pop_limit = 16u * (unsigned)slots;   // bound on block visits per point
   const unsigned nwork = list ? *list_count : (unsigned)npoints;
-  for (int i = lane; i < kWCap / 32; i += 32) W.queued[i] = 0u;
-  __syncwarp();
   for (;;) {
     unsigned w = 0;
     if (lane == 0) w = atomicAdd(sc.next_point, 1u);
@@ -1507,92 +1745,33 @@ wfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
     if (w >= nwork) break;
     const int p = list ? list[w] : (int)w;
     const PointIn pi = points[p];
-    if (lane == 0) {
-      const DevLens& D = lenses[pi.lens];
-      Ctx& c = W.c;
-      c.sx = pi.sx;
-      c.sy = pi.sy;
-      c.cx0 = D.g.corner_x;
-      c.cy0 = D.g.corner_y;
-      c.h = D.g.h;
-      c.n = D.g.n;
-      c.rho = D.rho;
-      c.rho2 = D.rho2;
-      c.ld_a = D.ld_a;
-      c.ld_b = D.ld_b;
-      c.m1 = D.L.m1;
-      c.m2 = D.L.m2;
-      c.m3 = D.L.m3;
-      c.z2x = D.L.z2.re;
-      c.z3x = D.L.z3.re;
-      c.z3y = D.L.z3.im;
-      c.binary = D.ray_binary;
-      c.txmax = (int)((c.n - 1) >> 5);
-      c.tymax = (int)((c.n - 1) >> 5);
-      c.split = split_mode;
-      // super-tile edge as the CTA fill: 2^9 pixels, down to 2^7 as h grows
-      int sl = 9;
-      while (sl > 7 && c.h * (double)(1 << sl) > 1.5e-3) sl--;
-      c.slog2 = sl;
-      c.hf = (float)c.h;
-      c.rho2f = (float)c.rho2;
-      c.inv_rho2f = (float)(1.0 / c.rho2);
-      c.ldaf = (float)c.ld_a;
-      c.ldbf = (float)c.ld_b;
-      W.top = 0;
-      W.used = 0;
-      W.nseed = 0;
-    }
-    if (lane < kWStCache) W.sttag[lane] = kEmptyKey;
-    __syncwarp();
+    w_context(W, pi, lenses, split_mode, lane);
     const int64_t n = W.c.n;
     uint32_t status = 0;
     if (!(n > 2 && n < ((int64_t)1 << 31)) || (out[p].status & kStBadInput)) status |= kStBadInput;
     else if (pi.est_blocks > sc.wthr) status |= kStTableFull;   // left to the CTA fill
-    WAcc A = {0ull, 0ull, 0ull, 0ll, 0u};
+    WAcc A = {0ull, 0ull, 0ull, 0ll, 0u, {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u}};
     unsigned pops = 0;
     if (!status) {
-      // seeds (lcirs.cc:171-174; seed rows must satisfy 0 < ny < N, 386-391)
-      const unsigned ns = min(out[p].nseeds, (unsigned)kMaxSeeds);
-      for (unsigned k0 = 0; k0 < ns; k0 += 32) {
-        const unsigned k = k0 + (unsigned)lane;
-        int32_t px = 0, py = 0;
-        bool ok = false, edge = false;
-        if (k < ns) {
-          px = seeds[((size_t)p * kMaxSeeds + k) * 2];
-          py = seeds[((size_t)p * kMaxSeeds + k) * 2 + 1];
-          if (py > 0 && (int64_t)py < n) {
-            if (px < 1 || (int64_t)px > n - 1) edge = true;
-            else ok = true;
-          }
-        }
-        if (__any_sync(kFull, edge)) status |= kStEdge;
-        const uint32_t okm = __ballot_sync(kFull, ok);
-        if (ok) {
-          const unsigned pos = W.nseed + (unsigned)__popc(okm & ((1u << lane) - 1u));
-          W.seedx[pos] = px;
-          W.seedy[pos] = py;
-        }
-        __syncwarp();
-        if (lane == 0) W.nseed += (unsigned)__popc(okm);
-        __syncwarp();
-      }
+      status |= w_load_seeds(W, p, seeds, out, lane);
       // seed blocks: found or inserted by group 0, marked and queued
       const unsigned nsd = W.nseed;
       for (unsigned k = 0; k < nsd; k++) {
         const int sbx = W.seedx[k] >> 5, sby = W.seedy[k] >> 5;
         bool ins = false;
-        const int s = w_find4(T, lane < 8, sbx, sby, lane, &ins);
+        unsigned rounds = 0;
+        const int s = w_find4(T, lane < 8, sbx, sby, lane, &ins, &rounds);
         if (lane < 8 && s >= 0 && ins) w_init_slot(W, T, s, sbx, sby, lane);
         __syncwarp();
         if (lane == 0 && s >= 0) {
           uint32_t* h = T.hdr + (size_t)s * kWHdrWords;
-          __stcg(&h[kHState], ldcg32(&h[kHState]) | kWSeed);
-          w_queue(W, T, (uint32_t)s);
+          const uint32_t st0 = ldcg32(&h[kHState]);
+          __stcg(&h[kHState], st0 | kWSeed | kWQueued);
+          if (!(st0 & kWQueued)) w_push_stack(W, T, (uint32_t)s);
         }
         __syncwarp();
         const int sl0 = __shfl_sync(kFull, s, 0);
-        if (sl0 < 0 || W.used > kWUsable) {
+        if (sl0 < 0 || W.used > T.usable) {
           status |= kStTableFull;
           break;
         }
@@ -1603,17 +1782,18 @@ wfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
         if (t == 0u) break;
         const uint32_t slot = t - 1u < (unsigned)kWStack ? W.stack[t - 1u] : ldcg32(&T.spill[t - 1u]);
         __syncwarp();
-        if (lane == 0) {
-          W.top = t - 1u;
-          W.queued[slot >> 5] &= ~(1u << (slot & 31u));
-        }
+        if (lane == 0) W.top = t - 1u;
         __syncwarp();
-        w_block(W, T, slot, lane, A);
-        if (W.used > kWUsable) status |= kStTableFull;
-        if (++pops > kWPopLimit) status |= kStTimeout;
+        w_block(W, T, slot, lane, A, nullptr);
+        if (W.used > T.usable) status |= kStTableFull;
+        if (++pops > pop_limit) status |= kStTimeout;
       }
     }
-    const unsigned nused = min(W.used, (unsigned)kWCap);
+    const unsigned nused = min(W.used, (unsigned)slots);
+    if (sc.prof && lane == 0) {
+      A.prof[7] = 1u;
+      for (int q = 0; q < 8; q++) atomicAdd(&sc.prof[q], (unsigned long long)A.prof[q]);
+    }
     if (lane == 0) {
       PointOut o = out[p];
       o.count = A.count;
@@ -1625,38 +1805,223 @@ wfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
       o.rays_fp64 = A.fp64;
       out[p] = o;
     }
-    // amoeba export (32 x 8 tiles of F, as the CTA fill) and the clearing
-    // of the slots used (the table starts every point empty)
-    const bool complete = !(status & (kStTableFull | kStTimeout | kStBadInput));
-    for (unsigned u = (unsigned)lane; u < nused; u += 32) {
-      const uint32_t slot = ldcg32(&T.used[u]);
-      if (sc.dump && complete) {
-        const uint32_t* h = T.hdr + (size_t)slot * kWHdrWords;
-        if (ldcg32(&h[kHState]) & kWCls) {
-          const uint32_t* b = T.body + (size_t)slot * 64;
-          const uint32_t bxk = ldcg32(&h[kHBx]), byk = ldcg32(&h[kHBy]);
-          for (int t8 = 0; t8 < 4; t8++) {
-            uint32_t fm[8], a8 = 0;
-            for (int r = 0; r < 8; r++) a8 |= (fm[r] = ldcg32(&b[32 + 8 * t8 + r]));
-            if (!a8) continue;
-            const unsigned d = atomicAdd(sc.dump_count, 1u);
-            if (d < sc.dump_cap) {
-              uint32_t* o = sc.dump + (size_t)d * kDumpWords;
-              o[0] = (uint32_t)p;
-              o[1] = bxk;
-              o[2] = byk * 4u + (uint32_t)t8;
-              for (int r = 0; r < 8; r++) o[3 + r] = fm[r];
-            }
+    // amoeba export and the clearing of the slots used (the table starts
+    // every point empty)
+    w_finish(T, sc, p, nused, !(status & (kStTableFull | kStTimeout | kStBadInput)), lane);
+    __syncwarp();
+  }
+}
+
+// ===========================================================================
+// Team fill: kTeamWarps warps of one CTA fill one large point together, in
+// rounds.  Each warp owns the blocks of its share of the super-tiles
+// (team_owner) in its own table and works them as the warp fill does; an
+// entry into a block of another share is a message in that warp's inbox.
+// A round: every warp reads the previous round's messages into its table,
+// the CTA meets at a barrier, every warp works its stack empty, the CTA
+// meets again, and another round runs while any message was sent.  The only
+// waits are these barriers, which every warp reaches once per round.
+// ===========================================================================
+namespace {
+constexpr int kTThreads = 32 * kTeamWarps;
+constexpr int kTeamRounds = 1 << 16;
+
+struct TeamSh {
+  WarpSh w[kTeamWarps];
+  unsigned inbox_n[2 * kTeamWarps];
+  unsigned abort_;          // kStTableFull / kStTimeout: the point ends
+  int point;
+  unsigned long long count, eval, fp64;
+  unsigned long long fx;    // two's complement sum of the warps' 2^-16 units
+  unsigned tiles, status;
+};
+}  // namespace
+
+template <int MINB>
+__global__ void __launch_bounds__(kTThreads, MINB)
+tfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const int32_t* seeds,
+             PointOut* out, WScratch sc, int split_mode, const int32_t* list,
+             const unsigned* list_count) {
+  __shared__ TeamSh S;
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  WarpSh& W = S.w[wid];
+  const WTable T = w_table(sc, (size_t)blockIdx.x * kTeamWarps + wid);
+  const size_t slots = (size_t)T.mask + 1;
+  const unsigned pop_limit = 16u * (unsigned)slots;   // block visits per warp and point
+  const unsigned nwork = list ? *list_count : (unsigned)npoints;
+  WTeam tm;
+  tm.inbox = sc.inbox + (size_t)blockIdx.x * 2 * kTeamWarps * sc.inbox_cap;
+  tm.inbox_n = S.inbox_n;
+  tm.abort_ = &S.abort_;
+  tm.cap = sc.inbox_cap;
+  tm.me = wid;
+  tm.post = 1;
+  tm.sh = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned w = atomicAdd(sc.next_point, 1u);
+      S.point = w < nwork ? (list ? list[w] : (int)w) : -1;
+      S.abort_ = 0u;
+      S.count = S.eval = S.fp64 = S.fx = 0ull;
+      S.tiles = 0u;
+      S.status = 0u;
+    }
+    if (threadIdx.x < 2 * kTeamWarps) S.inbox_n[threadIdx.x] = 0u;
+    __syncthreads();
+    const int p = S.point;
+    if (p < 0) break;
+    const PointIn pi = points[p];
+    w_context(W, pi, lenses, split_mode, lane);
+    tm.sh = W.c.slog2 - 5;
+    const int64_t n = W.c.n;
+    const bool skip = !(n > 2 && n < ((int64_t)1 << 31)) || (out[p].status & kStBadInput);
+    uint32_t status = skip ? (uint32_t)kStBadInput : 0u;
+    WAcc A = {0ull, 0ull, 0ull, 0ll, 0u, {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u}};
+    if (!skip) {
+      status |= w_load_seeds(W, p, seeds, out, lane);
+      // the seed blocks of this warp's share
+      const unsigned nsd = W.nseed;
+      for (unsigned k = 0; k < nsd; k++) {
+        const int sbx = W.seedx[k] >> 5, sby = W.seedy[k] >> 5;
+        if (team_owner(sbx, sby, tm.sh) != wid) continue;
+        bool ins = false;
+        unsigned rounds = 0;
+        const int s = w_find4(T, lane < 8, sbx, sby, lane, &ins, &rounds);
+        if (lane < 8 && s >= 0 && ins) w_init_slot(W, T, s, sbx, sby, lane);
+        __syncwarp();
+        if (lane == 0 && s >= 0) {
+          uint32_t* h = T.hdr + (size_t)s * kWHdrWords;
+          const uint32_t st0 = ldcg32(&h[kHState]);
+          __stcg(&h[kHState], st0 | kWSeed | kWQueued);
+          if (!(st0 & kWQueued)) w_push_stack(W, T, (uint32_t)s);
+        }
+        __syncwarp();
+        const int sl0 = __shfl_sync(kFull, s, 0);
+        if (sl0 < 0 || W.used > T.usable) {
+          if (lane == 0) atomicOr(&S.abort_, (unsigned)kStTableFull);
+          break;
+        }
+      }
+    }
+    unsigned pops = 0;
+    int round = 0;
+    for (;; round++) {
+      const int pin = round & 1;   // buffer holding the previous round's messages
+      tm.post = pin ^ 1;
+      // messages into this warp's share, one at a time (group 0 looks the
+      // block up; one lane applies the bits)
+      if (round > 0 && !skip) {
+        const unsigned nin = min(S.inbox_n[pin * kTeamWarps + wid], tm.cap);
+        const uint4* box = tm.inbox + ((size_t)pin * kTeamWarps + wid) * tm.cap;
+        for (unsigned k = 0; k < nin; k++) {
+          unsigned ab = 0;
+          if (lane == 0) ab = *(volatile unsigned*)&S.abort_;
+          if (__shfl_sync(kFull, ab, 0)) break;
+          const uint4 m = box[k];
+          bool ins = false;
+          unsigned rounds = 0;
+          const int s = w_find4(T, lane < 8, (int)m.x, (int)m.y, lane, &ins, &rounds);
+          if (lane < 8 && s >= 0 && ins) w_init_slot(W, T, s, (int)m.x, (int)m.y, lane);
+          __syncwarp();
+          if (lane == 0 && s >= 0) w_enter(W, T, s, ins, (int)m.z, m.w);
+          __syncwarp();
+          const int sl0 = __shfl_sync(kFull, s, 0);
+          if (sl0 < 0 || W.used > T.usable) {
+            if (lane == 0) atomicOr(&S.abort_, (unsigned)kStTableFull);
+            break;
           }
         }
       }
-      __stcg((unsigned long long*)&T.keys[slot], (unsigned long long)kEmptyKey);
+      __syncthreads();
+      // the messages are read: the buffer takes the next round's
+      if (threadIdx.x < kTeamWarps) S.inbox_n[pin * kTeamWarps + threadIdx.x] = 0u;
+      // this warp's blocks, last queued first
+      while (!skip) {
+        unsigned ab = 0;
+        if (lane == 0) ab = *(volatile unsigned*)&S.abort_;
+        if (__shfl_sync(kFull, ab, 0)) break;
+        const unsigned t = W.top;
+        if (t == 0u) break;
+        const uint32_t slot =
+            t - 1u < (unsigned)kWStack ? W.stack[t - 1u] : ldcg32(&T.spill[t - 1u]);
+        __syncwarp();
+        if (lane == 0) W.top = t - 1u;
+        __syncwarp();
+        w_block(W, T, slot, lane, A, &tm);
+        ++pops;
+        if (lane == 0) {
+          if (W.used > T.usable) atomicOr(&S.abort_, (unsigned)kStTableFull);
+          if (pops > pop_limit) atomicOr(&S.abort_, (unsigned)kStTimeout);
+        }
+      }
+      __syncthreads();
+      const bool ab = S.abort_ != 0u;
+      const int more =
+          __syncthreads_or(lane == 0 && S.inbox_n[tm.post * kTeamWarps + wid] != 0u);
+      if (ab || !more) break;
+      if (round + 1 >= kTeamRounds) {
+        if (threadIdx.x == 0) atomicOr(&S.abort_, (unsigned)kStTimeout);
+        break;
+      }
     }
-    // slots left queued by a point given up on
-    if (W.top != 0u)
-      for (int i = lane; i < kWCap / 32; i += 32) W.queued[i] = 0u;
-    __syncwarp();
+    // the point's totals
+    if (lane == 0) {
+      atomicAdd(&S.count, A.count);
+      atomicAdd(&S.eval, A.eval);
+      atomicAdd(&S.fp64, A.fp64);
+      atomicAdd(&S.fx, (unsigned long long)A.fx);
+      atomicAdd(&S.tiles, min(W.used, (unsigned)slots));
+      atomicOr(&S.status, status | (A.edge ? (uint32_t)kStEdge : 0u));
+    }
+    __syncthreads();
+    const uint32_t fin = S.status | S.abort_;
+    if (threadIdx.x == 0) {
+      PointOut o = out[p];
+      o.count = S.count;
+      o.wsum_fx = (int64_t)S.fx * 65536ll;
+      o.status |= fin;
+      o.tiles = S.tiles;
+      // rounds (bits 0-15) and the time limit (bit 16)
+      o.diag = (uint32_t)min(round + 1, 0xffff) | ((S.abort_ & kStTimeout) ? 0x10000u : 0u);
+      o.rays_eval = S.eval;
+      o.rays_fp64 = S.fp64;
+      out[p] = o;
+    }
+    w_finish(T, sc, p, min(W.used, (unsigned)slots),
+             !(fin & (kStTableFull | kStTimeout | kStBadInput)), lane);
+    __syncthreads();
   }
+}
+
+int tfill_default_teams() {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms * 2;
+}
+
+size_t tscratch_bytes(int teams, int cap_log2, unsigned inbox_cap) {
+  return wscratch_bytes(teams * kTeamWarps, cap_log2) +
+         (size_t)teams * 2 * kTeamWarps * inbox_cap * sizeof(uint4) + 256;
+}
+
+void tscratch_init(WScratch* s, void* base, int teams, int cap_log2, unsigned inbox_cap,
+                   cudaStream_t st) {
+  wscratch_init(s, base, teams * kTeamWarps, cap_log2, st);
+  const size_t wb = wscratch_bytes(teams * kTeamWarps, cap_log2);
+  s->inbox = (uint4*)(((uintptr_t)base + wb + 255) / 256 * 256);
+  s->inbox_cap = inbox_cap;
+}
+
+void launch_tfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
+                  const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
+                  cudaStream_t st, const int32_t* d_list, const unsigned* d_count) {
+  if (npoints <= 0 || s.warps < kTeamWarps) return;
+  cudaMemsetAsync(s.next_point, 0, sizeof(unsigned), st);
+  tfill_kernel<2><<<s.warps / kTeamWarps, kTThreads, 0, st>>>(
+      d_points, npoints, d_lenses, d_seeds, d_out, s, mode == kFillSplit ? 1 : 0, d_list,
+      d_count);
 }
 
 int wfill_default_warps() {
@@ -1666,15 +2031,16 @@ int wfill_default_warps() {
   return sms * kWOcc * kWWarps;
 }
 
-size_t wscratch_bytes(int warps) {
-  const size_t ent = (size_t)warps << kWCapLog2;
+size_t wscratch_bytes(int warps, int cap_log2) {
+  const size_t ent = (size_t)warps << cap_log2;
   return ent * (8 + (size_t)kWHdrWords * 4 + 64 * 4 + 4 + 4) + 256;
 }
 
-void wscratch_init(WScratch* s, void* base, int warps, cudaStream_t st) {
-  const size_t ent = (size_t)warps << kWCapLog2;
+void wscratch_init(WScratch* s, void* base, int warps, int cap_log2, cudaStream_t st) {
+  const size_t ent = (size_t)warps << cap_log2;
   char* p = (char*)base;
   s->warps = warps;
+  s->cap_log2 = cap_log2;
   s->keys = (uint64_t*)p;
   p += ent * 8;
   s->hdr = (uint32_t*)p;
@@ -1686,10 +2052,13 @@ void wscratch_init(WScratch* s, void* base, int warps, cudaStream_t st) {
   s->spill = (uint32_t*)p;
   p += ent * 4;
   s->next_point = (unsigned*)p;
-  s->wthr = 7000;
+  s->wthr = 14000;
   s->dump = nullptr;
   s->dump_count = nullptr;
   s->dump_cap = 0;
+  s->prof = nullptr;
+  s->inbox = nullptr;
+  s->inbox_cap = 0;
   // keys empty (all ones); headers are written when a slot is taken, bodies
   // are read only once their state says so
   cudaMemsetAsync(s->keys, 0xff, ent * 8, st);
