@@ -469,6 +469,8 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-config4", action="store_true")
     ap.add_argument("--no-noalloc", action="store_true")
+    ap.add_argument("--no-pipeline", action="store_true",
+                    help="exact chain: seeds then fill, not overlapped")
     ap.add_argument("--leg", choices=["config4", "surrogate"], default=None,
                     help="run one side leg alone and print its JSON object")
     ap.add_argument("--leg-timeout", type=int, default=300,
@@ -510,6 +512,8 @@ def main():
               "curves_per_gpu": args.curves, "points_per_curve": n + 1, "rho": 1e-3,
               "rays_per_radius": 500, "ld_v": 0.5, "seed": args.seed, "chain": chain_desc,
               "l2": "flushed between steps (256 MiB write)",
+              "overlap": ("exact chain in 8 segments, each segment's fill overlapped with the "
+                          "next segment's chain" if args.chain <= 0 else "none"),
               "parallelism": "curves sharded over %d GPU(s)" % world}
     ncpu = os.cpu_count() or 1
 
@@ -574,9 +578,19 @@ def main():
         bb.run_device(2, sptr)
         return e1
 
+    # the exact chain runs in segments overlapped with the fill (one call);
+    # the seeds/fill split for the roofline comes from a sequential step
+    pipelined = args.chain <= 0 and not args.no_pipeline
+
+    def step_timed(bb):
+        if pipelined:
+            bb.run_device(4, sptr)
+            return None
+        return step_device(bb)
+
     leg("inputs set: %d points" % npts)
     for _ in range(args.warmup):
-        step_device(b)
+        step_timed(b)
     torch.cuda.synchronize()
     leg("warm-up steps")
     amp, cnt, st = b.download(sptr)
@@ -598,13 +612,27 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e2 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            e1 = step_device(b)
+            e1 = step_timed(b)
             e2.record(stream)
             e2.synchronize()
             tot_ms += e0.elapsed_time(e2)
-            fill_ms += e1.elapsed_time(e2)
+            if e1 is not None:
+                fill_ms += e1.elapsed_time(e2)
         time.sleep(0.3)
     torch.cuda.synchronize()
+    seq_ms = None
+    if pipelined:
+        # one sequential step (seeds, then fill) for the seeds/fill split
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e2 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e1 = step_device(b)
+        e2.record(stream)
+        e2.synchronize()
+        seq_ms = e0.elapsed_time(e2)
+        fill_ms = e1.elapsed_time(e2) * args.steps
+        amp_seq, cnt_seq, _ = b.download(sptr)
     if dist:
         tot_ms = max_over_ranks(tot_ms, dist, "cuda")
         dist.barrier()
@@ -696,7 +724,10 @@ def main():
         "parity": parity_vs_fixture(cnt, n, len(lenses), args.seed, rank),
         "incomplete_points": incomplete,
         "status_counts": status_counts(st),
-        "seeds_ms_per_step": ms_step - fill_ms / args.steps,
+        "seeds_ms_per_step": (seq_ms if pipelined else ms_step) - fill_ms / args.steps,
+        "pipeline": ({"segments": 8, "sequential_ms_per_step": seq_ms,
+                      "counts_equal_sequential": bool(np.array_equal(cnt, cnt_seq))}
+                     if pipelined else None),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": achieved / peak_tf, "traffic": traffic,
                      "kernel": "wfill_kernel (+ fill_kernel for points above its table)",

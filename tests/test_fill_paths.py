@@ -7,10 +7,10 @@ stage that can hold it, so most points never see the later ones.  Here every
 path runs alone over the first curves of the bench workload (exact warm-start
 chain), in child processes with the engine's switches set, and each must give
 the reference's ray counts (strict IEEE build, tests/golden/bench_seed2024.npz)
-on every point, and the same magnifications within the limb-darkening
-tolerance of the other GPU tests.
+on every point, also when the chain runs in segments beside the fill, and the
+same magnifications within the limb-darkening tolerance of the other GPU
+tests.
 """
-import json
 import os
 import subprocess
 import sys
@@ -34,12 +34,15 @@ lenses, trajs, n = workloads.config2(2024, n_curves=%(curves)d, n_points=5000)
 b = Batch()
 b.set_chain(0)
 b.set_lenses(lenses)
-amp, cnt, st = b.run(trajs, np.arange(len(trajs)), np.full(len(trajs), n))
+b.set_trajectories(trajs, np.arange(len(trajs)), np.full(len(trajs), n))
+b.run_device(%(phase)d)
+amp, cnt, st = b.download()
 np.savez(%(out)r, amp=amp, cnt=cnt, st=st)
 """
 
 PATHS = {
     "default": {},
+    "overlapped": {"_phase": "4"},                      # chain in segments beside the fill
     "team": {"TL_WFILL_THR": "0"},                       # every point to the team fill
     "cta": {"TL_FILL_KERNEL": "cta"},                    # the CTA fill alone
     "cta_levels": {"TL_WFILL_THR": "0", "TL_TEAM_FILL": "0"},   # warp fill skips all
@@ -48,8 +51,9 @@ PATHS = {
 
 def _run(env_extra, out, product_lib):
     env = dict(os.environ)
-    env.update(env_extra)
-    code = _CHILD % {"root": ROOT, "curves": CURVES, "out": out}
+    env.update({k: v for k, v in env_extra.items() if not k.startswith("_")})
+    phase = int(env_extra.get("_phase", "3"))
+    code = _CHILD % {"root": ROOT, "curves": CURVES, "out": out, "phase": phase}
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]

@@ -77,6 +77,9 @@ int tlb_set_lenses(tl_batch* b, int nlens, const double* p8) {
   return nlens;
 }
 
+// segments of an exact chain for tlb_run_device phase 4
+constexpr int kSegments = 8;
+
 long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
                           const uint32_t* n) {
   if (!b || ntraj <= 0 || !t4 || !lens_idx || !n || b->nlens <= 0) return -1;
@@ -123,6 +126,49 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
                           E.stream));
   E.check(cudaMemcpyAsync(dj, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
+  // the exact chain in kSegments segments: jobs, point lists and counts
+  b->nseg = 0;
+  if (b->chain <= 0) {
+    const int S = kSegments;
+    std::vector<tl::SeedJob> sj;
+    std::vector<int32_t> sl;
+    std::vector<unsigned> sn(S, 0);
+    b->segoff.assign(S + 1, 0);
+    b->segjob0.assign(S + 1, 0);
+    for (int s = 0; s < S; s++) {
+      b->segjob0[s] = (int)sj.size();
+      b->segoff[s] = (int)sl.size();
+      for (int i = 0; i < ntraj; i++) {
+        const long np = (long)b->htraj[i].n + 1;
+        const long len = (np + S - 1) / S;
+        const long first = (long)s * len;
+        const long cnt = std::min(len, np - first);
+        if (cnt <= 0) continue;
+        tl::SeedJob j;
+        j.traj = i;
+        j.first = (int32_t)first;
+        j.count = (int32_t)cnt;
+        j.chain = i;   // the curve's chain, carried from segment to segment
+        sj.push_back(j);
+        for (long q = 0; q < cnt; q++) sl.push_back((int32_t)(b->htraj[i].point_base + first + q));
+      }
+      sn[s] = (unsigned)(sl.size() - b->segoff[s]);
+    }
+    b->segjob0[S] = (int)sj.size();
+    b->segoff[S] = (int)sl.size();
+    void* dsj = b->segjobs.need(sizeof(tl::SeedJob) * sj.size());
+    void* dsl = b->seglist.need(sizeof(int32_t) * sl.size());
+    void* dsn = b->segn.need(sizeof(unsigned) * S);
+    void* dch = b->chains.need(sizeof(tl::RootChain) * ntraj);
+    if (!dsj || !dsl || !dsn || !dch) return -2;
+    E.check(cudaMemcpyAsync(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(),
+                            cudaMemcpyHostToDevice, E.stream));
+    E.check(cudaMemcpyAsync(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
+                            E.stream));
+    E.check(cudaMemcpyAsync(dsn, sn.data(), sizeof(unsigned) * S, cudaMemcpyHostToDevice,
+                            E.stream));
+    b->nseg = S;
+  }
   if (!E.check(cudaStreamSynchronize(E.stream))) return -2;
   return base;
 }
@@ -143,6 +189,36 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
                      (const tl::DevLens*)b->lenses.p, (const cx*)b->ca.p, (tl::PointIn*)b->points.p,
                      (int32_t*)b->seeds.p, (tl::PointOut*)b->out.p, (tl::TrialList*)b->trials.p,
                      nullptr, st);
+  if ((phase & 4) && b->nscan > 0 && b->nseg > 0) {
+    // seeds and fill overlapped: the chain of segment s+1 runs while the
+    // warp fill works segment s
+    tl::Run R;
+    R.trajs = (tl::Traj*)b->trajs.p;
+    R.jobs = (tl::SeedJob*)b->jobs.p;
+    R.points = (tl::PointIn*)b->points.p;
+    R.seeds = (int32_t*)b->seeds.p;
+    R.out = (tl::PointOut*)b->out.p;
+    R.trials = (tl::TrialList*)b->trials.p;
+    R.dump = nullptr;
+    R.dump_count = nullptr;
+    R.dump_cap = 0;
+    tl::Pipeline P;
+    P.lenses = (const tl::DevLens*)b->lenses.p;
+    P.ca = (const cx*)b->ca.p;
+    P.scan = (const tl::SeedJob*)b->scan.p;
+    P.nscan = b->nscan;
+    P.ntraj = b->ntraj;
+    P.segjobs = (const tl::SeedJob*)b->segjobs.p;
+    P.segjob0 = b->segjob0.data();
+    P.seglist = (const int32_t*)b->seglist.p;
+    P.segoff = b->segoff.data();
+    P.segn = (const unsigned*)b->segn.p;
+    P.nseg = b->nseg;
+    P.prep = (tl::PointPrep*)b->prep.p;
+    P.chains = (tl::RootChain*)b->chains.p;
+    E.pipeline_exact(R, (size_t)b->npoints, P, b->precision, st);
+    return E.check(cudaGetLastError()) ? 0 : -2;
+  }
   if (phase & 2) {
     tl::Run R;
     R.trajs = (tl::Traj*)b->trajs.p;

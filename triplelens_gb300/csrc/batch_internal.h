@@ -17,6 +17,12 @@ struct tl_batch {
   int njobs = 0;
   tl::DevBuf trajs, jobs, points, seeds, out, amp, trials, scan, prep;
   int nscan = 0;                 // exact chain: point chunks of the scan/prep
+  // exact chain in segments (tlb_run_device phase 4): segment s holds one
+  // job per curve over its s-th share of points; its points are listed in
+  // seglist[segoff[s] .. segoff[s+1]) and counted in segn[s] (device)
+  int nseg = 0;
+  std::vector<int> segoff, segjob0;
+  tl::DevBuf segjobs, seglist, segn, chains;
   std::vector<tl::Traj> htraj;
   int precision = 1;
   int chain = tl::kChainChunk;   // warm-start chain length (<= 0: whole curve)

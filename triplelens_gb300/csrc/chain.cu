@@ -414,6 +414,42 @@ void launch_point_lc_exact(const Traj* d_trajs, const SeedJob* d_jobs, int njobs
   point_chain_kernel<<<njobs, 32, 0, st>>>(d_jobs, njobs, d_trajs, d_lenses, d_amp, d_chains);
 }
 
+namespace {
+// every curve's chain in the lens's construction state
+__global__ void chain_reset_kernel(const Traj* trajs, int ntraj, const DevLens* lenses,
+                                   RootChain* chains) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntraj) return;
+  RootChain ch;
+  chain_reset(&ch, lenses[trajs[t].lens].heap0);
+  chains[t] = ch;
+}
+}  // namespace
+
+void launch_seeds_prep(const SeedJob* d_scan_jobs, int nscan, const Traj* d_trajs,
+                       const DevLens* d_lenses, const cx* d_ca, TrialList* d_trials,
+                       PointPrep* d_prep, cudaStream_t st) {
+  if (nscan <= 0) return;
+  launch_caustic_scan(d_scan_jobs, nscan, d_trajs, d_lenses, d_ca, d_trials, st);
+  prep_kernel<<<(nscan + kPrepThreads - 1) / kPrepThreads, kPrepThreads, 0, st>>>(
+      d_scan_jobs, nscan, d_trajs, d_lenses, d_prep);
+}
+
+void launch_chain_reset(const Traj* d_trajs, int ntraj, const DevLens* d_lenses,
+                        RootChain* d_chains, cudaStream_t st) {
+  if (ntraj <= 0) return;
+  chain_reset_kernel<<<(ntraj + 127) / 128, 128, 0, st>>>(d_trajs, ntraj, d_lenses, d_chains);
+}
+
+void launch_chain(const SeedJob* d_chain_jobs, int nchain, const Traj* d_trajs,
+                  const DevLens* d_lenses, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
+                  const TrialList* d_trials, const PointPrep* d_prep, RootChain* d_chains,
+                  cudaStream_t st) {
+  if (nchain <= 0) return;
+  chain_kernel<<<nchain, 32, 0, st>>>(d_chain_jobs, nchain, d_trajs, d_lenses, d_points, d_seeds,
+                                      d_out, d_trials, d_prep, d_chains);
+}
+
 void launch_seeds_exact(const SeedJob* d_scan_jobs, int nscan, const SeedJob* d_chain_jobs,
                         int nchain, const Traj* d_trajs, const DevLens* d_lenses, const cx* d_ca,
                         PointIn* d_points, int32_t* d_seeds, PointOut* d_out,

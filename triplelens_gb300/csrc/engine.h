@@ -147,6 +147,19 @@ void launch_seeds_exact(const SeedJob* d_scan_jobs, int nscan, const SeedJob* d_
                         TrialList* d_trials, PointPrep* d_prep, RootChain* d_chains,
                         cudaStream_t st);
 void upload_chain_tables(const TrigTable& t);
+// the two parts of launch_seeds_exact, for chains run in segments: the
+// caustic scan and PointPrep of the scan jobs; the chain jobs (a job with
+// chain >= 0 starts from chains[chain] and leaves its state there)
+void launch_seeds_prep(const SeedJob* d_scan_jobs, int nscan, const Traj* d_trajs,
+                       const DevLens* d_lenses, const cx* d_ca, TrialList* d_trials,
+                       PointPrep* d_prep, cudaStream_t st);
+void launch_chain(const SeedJob* d_chain_jobs, int nchain, const Traj* d_trajs,
+                  const DevLens* d_lenses, PointIn* d_points, int32_t* d_seeds, PointOut* d_out,
+                  const TrialList* d_trials, const PointPrep* d_prep, RootChain* d_chains,
+                  cudaStream_t st);
+// chains[t] = the construction state of curve t's lens
+void launch_chain_reset(const Traj* d_trajs, int ntraj, const DevLens* d_lenses,
+                        RootChain* d_chains, cudaStream_t st);
 // point-source curve with one warm-start chain per job (chain.cu)
 void launch_point_lc_exact(const Traj* d_trajs, const SeedJob* d_jobs, int njobs,
                            const DevLens* d_lenses, double* d_amp, RootChain* d_chains,
@@ -273,10 +286,33 @@ void launch_tfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                   const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
                   cudaStream_t st, const int32_t* d_list = nullptr,
                   const unsigned* d_count = nullptr);
-// d_list/d_count (optional): process only the listed points
+// d_list/d_count (optional): process only the listed points.  ctas_per_sm
+// (1..7, 0: all 8) caps the resident CTAs per SM and leaves room for a
+// one-warp kernel of up to 255 registers beside them (the exact chain).
 void launch_wfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                   const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
                   cudaStream_t st, const int32_t* d_list = nullptr,
-                  const unsigned* d_count = nullptr);
+                  const unsigned* d_count = nullptr, int ctas_per_sm = 0);
+
+// Seeds and fill of an exact chain overlapped (Engine::pipeline_exact): the
+// chain runs in nseg segments (segjobs[segjob0[s] .. segjob0[s+1]) carry
+// every curve's state in chains), and while segment s+1's chain runs the
+// warp fill works segment s's points (seglist[segoff[s] ..), segn[s] on the
+// device).
+struct Pipeline {
+  const DevLens* lenses;
+  const cx* ca;
+  const SeedJob* scan;
+  int nscan;
+  int ntraj;
+  const SeedJob* segjobs;
+  const int* segjob0;      // host, nseg + 1
+  const int32_t* seglist;
+  const int* segoff;       // host, nseg + 1
+  const unsigned* segn;    // device, nseg
+  int nseg;
+  PointPrep* prep;
+  RootChain* chains;
+};
 
 }  // namespace tl

@@ -90,6 +90,8 @@ Engine::Engine() {
   // TL_TEAM_FILL=0: no team fill (the CTA fill takes the warp fill's leftovers);
   // TL_TEAMS: teams of 8 warps (default 2 per SM)
   if (const char* c = getenv("TL_TEAM_FILL")) team_fill_ = atoi(c) != 0;
+  // TL_PIPE_CTAS: warp-fill CTAs per SM beside the chain (1..7)
+  if (const char* c = getenv("TL_PIPE_CTAS")) pipe_ctas_ = atoi(c);
   if (const char* c = getenv("TL_TEAMS")) want_teams_ = atoi(c);
   // TL_WFILL_CAP_LOG2: slots per warp table (10..14; the threshold follows)
   if (const char* c = getenv("TL_WFILL_CAP_LOG2")) {
@@ -247,12 +249,6 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
   unsigned* order_meta = (unsigned*)ob;
   int32_t* order_list = (int32_t*)(ob + 1024);
   launch_order(R.points, (int)np, order_list, order_meta, big_units_, st);
-  // points left over by one stage (status bit 4) are listed for the next;
-  // the launches read their point count on the device, so no host round trip
-  // is needed (a launch with an empty list exits at once)
-  char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
-  int32_t* list = (int32_t*)(rb + 64);
-  unsigned* count = (unsigned*)rb;
   cudaEvent_t pe[3] = {nullptr, nullptr, nullptr};
   if (profiling && warp) {
     for (auto& e : pe) cudaEventCreate(&e);
@@ -283,15 +279,6 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
               "probe rounds %llu  inserted %llu  whole %llu  ray-by-ray weights %llu\n",
               h[7], h[0], h[1], h[2], h[3], h[4], h[5], h[6]);
     }
-    if (team) {
-      // the larger points (and those whose warp table filled up): 8 warps each
-      WScratch t = ts_;
-      t.dump = R.dump;
-      t.dump_count = R.dump_count;
-      t.dump_cap = R.dump_cap;
-      launch_collect_overflow(R.out, (int)np, list, count, st);
-      launch_tfill(R.points, (int)np, d_lenses, R.seeds, R.out, t, mode, st, list, count);
-    }
   } else {
     FillScratch s = fs_[0];
     s.nbig = order_meta + 1;
@@ -319,6 +306,42 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     }
   }
   if (profiling && warp) cudaEventRecord(pe[2], st);
+  fill_rest(R, np, d_lenses, mode, st, warp, team);
+  if (profiling && warp) {
+    cudaEvent_t e3;
+    cudaEventCreate(&e3);
+    cudaEventRecord(e3, st);
+    cudaEventSynchronize(e3);
+    float a = 0.f, b = 0.f, c = 0.f;
+    cudaEventElapsedTime(&a, pe[0], pe[1]);
+    cudaEventElapsedTime(&b, pe[1], pe[2]);
+    cudaEventElapsedTime(&c, pe[2], e3);
+    fprintf(stderr, "[tl wprof] warp fill %.1f ms, then %.1f ms, team fill and CTA-fill levels %.1f ms\n",
+            a, b, c);
+    for (auto& e : pe) cudaEventDestroy(e);
+    cudaEventDestroy(e3);
+  }
+  if (!capturing) fill_mark(st);
+  check(cudaGetLastError());
+}
+
+void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mode,
+                       cudaStream_t st, bool warp, bool team) {
+  // points left over by one stage (status bit 4) are listed for the next;
+  // the launches read their point count on the device, so no host round trip
+  // is needed (a launch with an empty list exits at once)
+  char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
+  int32_t* list = (int32_t*)(rb + 64);
+  unsigned* count = (unsigned*)rb;
+  if (warp && team) {
+    // the larger points (and those whose warp table filled up): 8 warps each
+    WScratch t = ts_;
+    t.dump = R.dump;
+    t.dump_count = R.dump_count;
+    t.dump_cap = R.dump_cap;
+    launch_collect_overflow(R.out, (int)np, list, count, st);
+    launch_tfill(R.points, (int)np, d_lenses, R.seeds, R.out, t, mode, st, list, count);
+  }
   // points whose table overflowed run again with larger tables (CTA fill;
   // level 0 only when neither the team fill nor the CTA fill has run)
   for (int level = warp && !team ? 0 : 1; level < kFillLevels && level < levels_; level++) {
@@ -331,21 +354,83 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     launch_collect_overflow(R.out, (int)np, list, count, st);
     launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, sl, mode, threads_, st, list, count);
   }
-  if (profiling && warp) {
-    cudaEvent_t e3;
-    cudaEventCreate(&e3);
-    cudaEventRecord(e3, st);
-    cudaEventSynchronize(e3);
-    float a = 0.f, b = 0.f, c = 0.f;
-    cudaEventElapsedTime(&a, pe[0], pe[1]);
-    cudaEventElapsedTime(&b, pe[1], pe[2]);
-    cudaEventElapsedTime(&c, pe[2], e3);
-    fprintf(stderr, "[tl wprof] warp fill %.1f ms, team fill %.1f ms, CTA-fill levels %.1f ms\n",
-            a, b, c);
-    for (auto& e : pe) cudaEventDestroy(e);
-    cudaEventDestroy(e3);
+}
+
+void Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode,
+                            cudaStream_t st) {
+  const bool team = team_fill_ != 0;
+  if (!ensure_wscratch()) return;
+  if (team && !ensure_tscratch()) return;
+  if (!team && !ensure_fill_scratch(0)) return;
+  if (!side_ && !check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking))) return;
+  while ((int)seg_ev_.size() < P.nseg + 1) {
+    cudaEvent_t e;
+    if (!check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return;
+    seg_ev_.push_back(e);
   }
-  if (!capturing) fill_mark(st);
+  fill_after(st);
+  launch_seeds_prep(P.scan, P.nscan, R.trajs, P.lenses, P.ca, R.trials, P.prep, st);
+  launch_chain_reset(R.trajs, P.ntraj, P.lenses, P.chains, st);
+  WScratch w = ws_;
+  w.wthr = wfill_thr_;
+  w.dump = R.dump;
+  w.dump_count = R.dump_count;
+  w.dump_cap = R.dump_cap;
+  // TL_FILL_PROFILE: event times of the chain segments and the fills
+  std::vector<cudaEvent_t> tc, tf;
+  cudaEvent_t t0 = nullptr, tend = nullptr;
+  if (profiling) {
+    cudaEventCreate(&t0);
+    cudaEventCreate(&tend);
+    cudaEventRecord(t0, st);
+    tc.resize(P.nseg);
+    tf.resize(P.nseg);
+    for (int s = 0; s < P.nseg; s++) {
+      cudaEventCreate(&tc[s]);
+      cudaEventCreate(&tf[s]);
+    }
+  }
+  for (int s = 0; s < P.nseg; s++) {
+    launch_chain(P.segjobs + P.segjob0[s], P.segjob0[s + 1] - P.segjob0[s], R.trajs, P.lenses,
+                 R.points, R.seeds, R.out, R.trials, P.prep, P.chains, st);
+    if (profiling) cudaEventRecord(tc[s], st);
+    check(cudaEventRecord(seg_ev_[s], st));
+    check(cudaStreamWaitEvent(side_, seg_ev_[s], 0));
+    // wfill_ctas_ CTAs per SM: every SM keeps room for the next segment's
+    // chain warp
+    launch_wfill(R.points, (int)np, P.lenses, R.seeds, R.out, w, mode, side_,
+                 P.seglist + P.segoff[s], P.segn + s, pipe_ctas_);
+    if (profiling) cudaEventRecord(tf[s], side_);
+  }
+  check(cudaEventRecord(seg_ev_[P.nseg], side_));
+  check(cudaStreamWaitEvent(st, seg_ev_[P.nseg], 0));
+  fill_rest(R, np, P.lenses, mode, st, true, team);
+  fill_mark(st);
+  if (profiling) {
+    cudaEventRecord(tend, st);
+    cudaEventSynchronize(tend);
+    fprintf(stderr, "[tl pipe] chain segments end at");
+    for (int s = 0; s < P.nseg; s++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, t0, tc[s]);
+      fprintf(stderr, " %.0f", ms);
+    }
+    fprintf(stderr, " ms; fills end at");
+    for (int s = 0; s < P.nseg; s++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, t0, tf[s]);
+      fprintf(stderr, " %.0f", ms);
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, tend);
+    fprintf(stderr, " ms; all %.0f ms\n", ms);
+    for (int s = 0; s < P.nseg; s++) {
+      cudaEventDestroy(tc[s]);
+      cudaEventDestroy(tf[s]);
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(tend);
+  }
   check(cudaGetLastError());
 }
 

@@ -8,6 +8,7 @@
 
 #include <cstdio>
 #include <mutex>
+#include <vector>
 
 #include "engine.h"
 
@@ -75,6 +76,9 @@ class Engine {
   // stream either was launched on.  Call with `mu` held.
   void fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
   void fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
+  // seeds (exact chain, in segments) and fill overlapped on st and a side
+  // stream; the result is ordered on st
+  void pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode, cudaStream_t st);
   // order work that uses the fill tables outside fill_on (a graph replay):
   // fill_after makes st wait for the last fill, fill_mark records st's work
   // as the last fill
@@ -107,6 +111,13 @@ class Engine {
   int wfill_cap_log2_ = 14;
   // the team fill (8 warps per point) takes the points the warp fill leaves
   bool ensure_tscratch();
+  // the leftovers of the warp fill (status bit 4): team fill, then the
+  // CTA-fill levels; rb: the retry buffer
+  void fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st,
+                 bool warp, bool team);
+  cudaStream_t side_ = nullptr;
+  int pipe_ctas_ = 7;
+  std::vector<cudaEvent_t> seg_ev_;
   void* tfill_base_ = nullptr;
   WScratch ts_{};
   int team_fill_ = 1;

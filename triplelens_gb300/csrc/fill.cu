@@ -32,6 +32,8 @@
 // CTA abandons that point.  A full table sets kStTableFull (the host retries
 // those points with larger tables).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include <cmath>
@@ -2067,12 +2069,35 @@ void wscratch_init(WScratch* s, void* base, int warps, int cap_log2, cudaStream_
 
 void launch_wfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
                   const int32_t* d_seeds, PointOut* d_out, const WScratch& s, int mode,
-                  cudaStream_t st, const int32_t* d_list, const unsigned* d_count) {
+                  cudaStream_t st, const int32_t* d_list, const unsigned* d_count,
+                  int ctas_per_sm) {
   if (npoints <= 0 || s.warps <= 0) return;
   cudaMemsetAsync(s.next_point, 0, sizeof(unsigned), st);
-  const int ctas = (s.warps + kWWarps - 1) / kWWarps;
-  wfill_kernel<kWOcc><<<ctas, kWThreads, 0, st>>>(d_points, npoints, d_lenses, d_seeds, d_out, s,
-                                                  mode == kFillSplit ? 1 : 0, d_list, d_count);
+  int ctas = (s.warps + kWWarps - 1) / kWWarps;
+  size_t pad = 0;
+  if (ctas_per_sm > 0 && ctas_per_sm < kWOcc) {
+    int dev = 0, sms = 152, smem = 228 * 1024;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    int reserve = 1024;
+    cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    ctas = std::min(ctas, sms * ctas_per_sm);
+    // unused dynamic shared memory so that no SM takes more CTAs than that:
+    // (ctas_per_sm + 1) of them would exceed the SM's shared memory
+    const size_t per = (size_t)smem / (size_t)(ctas_per_sm + 1) + 1;
+    const size_t used = sizeof(WarpSh) * kWWarps + (size_t)reserve;
+    pad = per > used ? per - used : 0;
+    static bool carveout = false;
+    if (!carveout) {
+      cudaFuncSetAttribute(wfill_kernel<kWOcc>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           100);
+      carveout = true;
+    }
+  }
+  wfill_kernel<kWOcc><<<ctas, kWThreads, pad, st>>>(d_points, npoints, d_lenses, d_seeds, d_out,
+                                                    s, mode == kFillSplit ? 1 : 0, d_list,
+                                                    d_count);
 }
 
 int block_rec_words(int bh) {
