@@ -200,8 +200,9 @@ def hbm_view(traffic_bytes, fill_s, peaks):
 def config4_leg(seed, curves, reps):
     """Config 4 (sub-sample): `curves` light curves of 2000 points, each its
     own random lens with rho log-uniform in [1e-4, 3e-2], 200/500/1000 rays
-    per radius and v in [0.3, 0.7]; launch shape from the autotuner; seeds +
-    fill replayed as one CUDA graph (device-resident inputs)."""
+    per radius and v in [0.3, 0.7]; the fill stages' sharing of the points
+    from the autotuner; seeds + fill replayed as one CUDA graph
+    (device-resident inputs)."""
     import torch
     from triplelens_gb300 import workloads
     from triplelens_gb300.batch import Batch
@@ -236,10 +237,13 @@ def config4_leg(seed, curves, reps):
             "points": int(npts), "ms_per_replay": ms_graph, "points_per_s": npts / (ms_graph / 1e3),
             "rays_evaluated_per_s": float(stats[0]) / (ms_graph / 1e3),
             "ms_plain_launches": ms_plain,
-            "autotune": {"block_h": chosen[0], "ctas_per_sm": chosen[1], "points_timed": chosen[2],
-                         "candidates_ms": {"32x2": float(times[0]), "32x3": float(times[1]),
-                                           "32x4": float(times[2]), "16x2": float(times[3]),
-                                           "8x2": float(times[4])},
+            "autotune": {"warp_fill_threshold_blocks": chosen[0], "team_fill": bool(chosen[1]),
+                         "points_timed": chosen[2],
+                         "candidates_ms": {"warp<=7000+team": float(times[0]),
+                                           "warp<=3000+team": float(times[1]),
+                                           "warp<=1500+team": float(times[2]),
+                                           "warp<=7000+cta": float(times[3]),
+                                           "cta": float(times[4])},
                          "seconds": round(t_tune, 2)},
             "status_or": int(np.bitwise_or.reduce(st))}
 

@@ -81,13 +81,15 @@ int tlb_set_chain(tl_batch* b, int points);
 long tlb_point_lc(tl_batch* b, double* amp);
 
 /* Autotuner: runs the seeds of the current trajectories, then times the
- * fill over their first sample_points points (all if <= 0) for the launch
- * shapes (block height = rows of the 32-column frontier blocks, resident
- * fill CTAs per SM) (32, 2), (32, 3), (32, 4), (16, 2), (8, 2), and keeps
- * the fastest for later runs of the process.  chosen3 = {block height, CTAs
- * per SM, points timed}; times_ms (5 floats, may be NULL) the fill times in
- * that order.  Results do not depend on the choice (the filled sets are
- * exact). */
+ * fill over their first sample_points points (all if <= 0) for five ways of
+ * sharing the points among the fill's stages by predicted size (blocks of
+ * 32 x 32 rays): one warp per point up to 7000, 3000 or 1500 blocks and a
+ * team of 8 warps per larger point; one warp up to 7000 and the CTA fill for
+ * larger points; the CTA fill alone.  Keeps the fastest for later runs of the
+ * process.  chosen3 = {warp-fill threshold in blocks (0: CTA fill alone),
+ * 1 if the team fill takes the larger points, points timed}; times_ms (5
+ * floats, may be NULL) the fill times in that order.  Results do not depend
+ * on the choice (the filled sets are exact). */
 int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times_ms);
 
 /* Captures seeds + fill of the current trajectories (one warm run first,

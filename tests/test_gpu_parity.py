@@ -317,7 +317,7 @@ def test_config3_caustic_crossing(product_lib, oracle_lib, precision):
 def test_config4_graph_and_autotune(product_lib):
     """Config 4 (sub-sample: 8 curves x 301 points, each its own lens, rho
     log-uniform in [1e-4, 3e-2], 200/500/1000 rays per radius): the counts
-    do not depend on the autotuner's launch shape, and a CUDA-graph replay
+    do not depend on the autotuner's choice of fill stages, and a CUDA-graph replay
     gives the plain run's counts, also after the trajectories are replaced."""
     from triplelens_gb300.batch import Batch
     lenses, trajs, _ = workloads.config4(3, n_curves=8)
@@ -330,7 +330,7 @@ def test_config4_graph_and_autotune(product_lib):
     amp0, cnt0, st0 = b.download()
     assert np.bitwise_or.reduce(st0) & 0x2d == 0
     chosen, times = b.autotune(sample_points=1000)
-    assert chosen[0] in (8, 16, 32) and chosen[1] in (2, 3, 4)
+    assert (chosen[0], chosen[1]) in ((7000, 1), (3000, 1), (1500, 1), (7000, 0), (0, 0))
     assert np.all(times[times >= 0] > 0)
     b.run_device(3)
     amp1, cnt1, _ = b.download()

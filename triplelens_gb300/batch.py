@@ -132,8 +132,11 @@ class Batch:
         return out
 
     def autotune(self, sample_points=0):
-        """Fastest fill launch shape on a prefix of the current points:
-        (block height, CTAs per SM, points timed), and the 5 timings (ms)."""
+        """Fastest sharing of the points among the fill's stages, timed on a
+        prefix of the current points: (warp-fill threshold in blocks, 0 for
+        the CTA fill alone; 1 if the team fill takes the larger points;
+        points timed), and the 5 timings (ms), in the order of
+        include/tl_batch.h."""
         chosen = np.zeros(3, np.int32)
         times = np.zeros(5, np.float32)
         r = self.L.tlb_autotune(self.obj, sample_points, chosen, times)

@@ -304,56 +304,55 @@ int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times
   const long np = sample_points > 0 && sample_points < b->npoints ? sample_points : b->npoints;
   // seeds of every point once; candidates time the fill of the first np
   if (tlb_run_device(b, 1, nullptr) < 0) return -2;
-  // the 8- and 16-row kernels are compiled for 2 CTAs per SM only
-  const int cand[5][2] = {{32, 2}, {32, 3}, {32, 4}, {16, 2}, {8, 2}};
+  // where the points go, by predicted size: one warp per point up to a
+  // threshold (blocks of 32 x 32 rays), then 8 warps per point (team fill)
+  // or the CTA fill; {threshold, team} (threshold 0: the CTA fill alone)
+  const int cand[5][2] = {{7000, 1}, {3000, 1}, {1500, 1}, {7000, 0}, {0, 0}};
   float best = 3.0e38f;
-  int best_bh = E.block_h(), best_occ = tl::fill_occupancy();
+  int best_thr = 7000, best_team = 1;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   int k = 0;
   for (const auto& c : cand) {
+    float ms = -1.f;
     {
-      const int bh = c[0], occ = c[1];
-      float ms = -1.f;
-      {
-        std::lock_guard<std::mutex> g(E.mu);
-        E.set_fill_config(0, 0, 0, bh, occ);
-        tl::Run R;
-        R.trajs = (tl::Traj*)b->trajs.p;
-        R.jobs = (tl::SeedJob*)b->jobs.p;
-        R.points = (tl::PointIn*)b->points.p;
-        R.seeds = (int32_t*)b->seeds.p;
-        R.out = (tl::PointOut*)b->out.p;
-        R.trials = (tl::TrialList*)b->trials.p;
-        R.dump = nullptr;
-        R.dump_count = nullptr;
-        R.dump_cap = 0;
-        for (int rep = 0; rep < 2; rep++) {   // the first run allocates the tables
-          cudaEventRecord(e0, E.stream);
-          E.fill_on(R, (size_t)np, (const tl::DevLens*)b->lenses.p, b->precision, E.stream);
-          cudaEventRecord(e1, E.stream);
-          if (!E.check(cudaEventSynchronize(e1))) break;
-          cudaEventElapsedTime(&ms, e0, e1);
-        }
+      std::lock_guard<std::mutex> g(E.mu);
+      E.set_fill_paths(c[0] > 0, c[1] != 0, (unsigned)c[0]);
+      tl::Run R;
+      R.trajs = (tl::Traj*)b->trajs.p;
+      R.jobs = (tl::SeedJob*)b->jobs.p;
+      R.points = (tl::PointIn*)b->points.p;
+      R.seeds = (int32_t*)b->seeds.p;
+      R.out = (tl::PointOut*)b->out.p;
+      R.trials = (tl::TrialList*)b->trials.p;
+      R.dump = nullptr;
+      R.dump_count = nullptr;
+      R.dump_cap = 0;
+      for (int rep = 0; rep < 2; rep++) {   // the first run allocates the tables
+        cudaEventRecord(e0, E.stream);
+        E.fill_on(R, (size_t)np, (const tl::DevLens*)b->lenses.p, b->precision, E.stream);
+        cudaEventRecord(e1, E.stream);
+        if (!E.check(cudaEventSynchronize(e1))) break;
+        cudaEventElapsedTime(&ms, e0, e1);
       }
-      if (times_ms) times_ms[k] = ms;
-      k++;
-      if (ms > 0.f && ms < best) {
-        best = ms;
-        best_bh = bh;
-        best_occ = occ;
-      }
+    }
+    if (times_ms) times_ms[k] = ms;
+    k++;
+    if (ms > 0.f && ms < best) {
+      best = ms;
+      best_thr = c[0];
+      best_team = c[1];
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   {
     std::lock_guard<std::mutex> g(E.mu);
-    E.set_fill_config(0, 0, 0, best_bh, best_occ);
+    E.set_fill_paths(best_thr > 0, best_team != 0, (unsigned)best_thr);
   }
-  chosen3[0] = best_bh;
-  chosen3[1] = best_occ;
+  chosen3[0] = best_thr;
+  chosen3[1] = best_team;
   chosen3[2] = (int32_t)np;
   return 0;
 }

@@ -190,7 +190,7 @@ bool Engine::ensure_tscratch() {
   if (ts_.keys) return true;
   const int teams = want_teams_ > 0 ? want_teams_ : tfill_default_teams();
   const int cap = kTeamCapLog2;
-  const unsigned inbox = 1u << 14;
+  const unsigned inbox = 1u << 13;
   if (!check(cudaMalloc(&tfill_base_, tscratch_bytes(teams, cap, inbox)))) return false;
   tscratch_init(&ts_, tfill_base_, teams, cap, inbox, stream);
   check(cudaStreamSynchronize(stream));

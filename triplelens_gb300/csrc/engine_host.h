@@ -96,6 +96,13 @@ class Engine {
   // rows per block (8, 16 or 32), occ the resident CTAs per SM (2, 3 or 4)
   void set_fill_config(int ctas, int cap_log2, int threads, int block_h = 0, int occ = 0);
   int block_h() const { return block_h_; }
+  // which stage takes which points: warp fill up to thr predicted blocks,
+  // then the team fill (team) or the CTA fill; warp = false: CTA fill alone
+  void set_fill_paths(bool warp, bool team, unsigned thr) {
+    warp_fill_ = warp ? 1 : 0;
+    team_fill_ = team ? 1 : 0;
+    if (thr > 0) wfill_thr_ = thr;
+  }
 
  private:
   Engine();

@@ -1593,11 +1593,18 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
   if (s >= 0 && j == 0) w_enter(W, T, s, ins, g, bits);
   if (remote && j == 0) {
     const unsigned k = atomicAdd(&tm->inbox_n[tm->post * kTeamWarps + owner], 1u);
-    if (k < tm->cap)
-      tm->inbox[((size_t)tm->post * kTeamWarps + owner) * tm->cap + k] =
-          make_uint4((uint32_t)nbx, (uint32_t)nby, (uint32_t)g, bits);
-    else
+    if (k < tm->cap) {
+      // the bits word last, after a CTA-scope fence: the owner may read the
+      // message in this round as soon as it sees bits (never 0 in a message)
+      uint32_t* mw = (uint32_t*)&tm->inbox[((size_t)tm->post * kTeamWarps + owner) * tm->cap + k];
+      __stcg(&mw[0], (uint32_t)nbx);
+      __stcg(&mw[1], (uint32_t)nby);
+      __stcg(&mw[2], (uint32_t)g);
+      __threadfence_block();
+      __stcg(&mw[3], bits);
+    } else {
       atomicOr(tm->abort_, (unsigned)kStTableFull);
+    }
   }
   __syncwarp();
 }
@@ -1830,7 +1837,8 @@ constexpr int kTeamRounds = 1 << 16;
 
 struct TeamSh {
   WarpSh w[kTeamWarps];
-  unsigned inbox_n[2 * kTeamWarps];
+  unsigned inbox_n[2 * kTeamWarps];    // messages reserved per inbox
+  unsigned inbox_rd[2 * kTeamWarps];   // messages read by the owner
   unsigned abort_;          // kStTableFull / kStTimeout: the point ends
   int point;
   unsigned long long count, eval, fp64;
@@ -1838,6 +1846,62 @@ struct TeamSh {
   unsigned tiles, status;
 };
 }  // namespace
+
+// whole warp: the messages of inbox buffer b that this warp has not read,
+// in order, up to the first one not yet written; returns how many it took.
+// Each message is looked up by group 0 and applied by one lane; its bits
+// word is cleared (the slot reads "unwritten" when the buffer is reused).
+__device__ __noinline__ unsigned team_drain(TeamSh& S, WarpSh& W, const WTable& T,
+                                            const WTeam& tm, int b, int wid, int lane) {
+  uint4* box = tm.inbox + ((size_t)b * kTeamWarps + wid) * tm.cap;
+  unsigned* rd = &S.inbox_rd[b * kTeamWarps + wid];
+  unsigned took = 0;
+  for (;;) {
+    unsigned k = 0, n = 0, ab = 0;
+    if (lane == 0) {
+      k = *(volatile unsigned*)rd;
+      n = min(*(volatile unsigned*)&S.inbox_n[b * kTeamWarps + wid], tm.cap);
+      ab = *(volatile unsigned*)&S.abort_;
+    }
+    k = __shfl_sync(kFull, k, 0);
+    n = __shfl_sync(kFull, n, 0);
+    if (__shfl_sync(kFull, ab, 0) || k >= n) break;
+    uint32_t* mw = (uint32_t*)&box[k];
+    uint32_t bits = 0, mx = 0, my = 0, side = 0;
+    if (lane == 0) {
+      bits = __ldcg(&mw[3]);   // from L2: the sender's stores go there
+      if (bits) {
+        __threadfence_block();
+        mx = __ldcg(&mw[0]);
+        my = __ldcg(&mw[1]);
+        side = __ldcg(&mw[2]);
+      }
+    }
+    bits = __shfl_sync(kFull, bits, 0);
+    if (!bits) break;   // reserved, not written yet: read in a later pass
+    mx = __shfl_sync(kFull, mx, 0);
+    my = __shfl_sync(kFull, my, 0);
+    side = __shfl_sync(kFull, side, 0);
+    bool ins = false;
+    unsigned rounds = 0;
+    const int s = w_find4(T, lane < 8, (int)mx, (int)my, lane, &ins, &rounds);
+    if (lane < 8 && s >= 0 && ins) w_init_slot(W, T, s, (int)mx, (int)my, lane);
+    __syncwarp();
+    if (lane == 0) {
+      if (s >= 0) w_enter(W, T, s, ins, (int)side, bits);
+      __stcg(&mw[3], 0u);
+      *rd = k + 1u;
+    }
+    __syncwarp();
+    took++;
+    const int sl0 = __shfl_sync(kFull, s, 0);
+    if (sl0 < 0 || W.used > T.usable) {
+      if (lane == 0) atomicOr(&S.abort_, (unsigned)kStTableFull);
+      break;
+    }
+  }
+  return took;
+}
 
 template <int MINB>
 __global__ void __launch_bounds__(kTThreads, MINB)
@@ -1869,7 +1933,10 @@ tfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
       S.tiles = 0u;
       S.status = 0u;
     }
-    if (threadIdx.x < 2 * kTeamWarps) S.inbox_n[threadIdx.x] = 0u;
+    if (threadIdx.x < 2 * kTeamWarps) {
+      S.inbox_n[threadIdx.x] = 0u;
+      S.inbox_rd[threadIdx.x] = 0u;
+    }
     __syncthreads();
     const int p = S.point;
     if (p < 0) break;
@@ -1911,56 +1978,42 @@ tfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
     for (;; round++) {
       const int pin = round & 1;   // buffer holding the previous round's messages
       tm.post = pin ^ 1;
-      // messages into this warp's share, one at a time (group 0 looks the
-      // block up; one lane applies the bits)
-      if (round > 0 && !skip) {
-        const unsigned nin = min(S.inbox_n[pin * kTeamWarps + wid], tm.cap);
-        const uint4* box = tm.inbox + ((size_t)pin * kTeamWarps + wid) * tm.cap;
-        for (unsigned k = 0; k < nin; k++) {
+      // the previous round's messages not read yet (all written: the
+      // barrier that ended the round orders them)
+      if (round > 0 && !skip) team_drain(S, W, T, tm, pin, wid, lane);
+      __syncthreads();
+      // the buffer is read out: it takes the next round's messages
+      if (threadIdx.x < kTeamWarps) {
+        S.inbox_n[pin * kTeamWarps + threadIdx.x] = 0u;
+        S.inbox_rd[pin * kTeamWarps + threadIdx.x] = 0u;
+      }
+      // this warp's blocks, last queued first, and the messages other warps
+      // send it meanwhile, until both run dry
+      for (;;) {
+        while (!skip) {
           unsigned ab = 0;
           if (lane == 0) ab = *(volatile unsigned*)&S.abort_;
           if (__shfl_sync(kFull, ab, 0)) break;
-          const uint4 m = box[k];
-          bool ins = false;
-          unsigned rounds = 0;
-          const int s = w_find4(T, lane < 8, (int)m.x, (int)m.y, lane, &ins, &rounds);
-          if (lane < 8 && s >= 0 && ins) w_init_slot(W, T, s, (int)m.x, (int)m.y, lane);
+          const unsigned t = W.top;
+          if (t == 0u) break;
+          const uint32_t slot =
+              t - 1u < (unsigned)kWStack ? W.stack[t - 1u] : ldcg32(&T.spill[t - 1u]);
           __syncwarp();
-          if (lane == 0 && s >= 0) w_enter(W, T, s, ins, (int)m.z, m.w);
+          if (lane == 0) W.top = t - 1u;
           __syncwarp();
-          const int sl0 = __shfl_sync(kFull, s, 0);
-          if (sl0 < 0 || W.used > T.usable) {
-            if (lane == 0) atomicOr(&S.abort_, (unsigned)kStTableFull);
-            break;
+          w_block(W, T, slot, lane, A, &tm);
+          ++pops;
+          if (lane == 0) {
+            if (W.used > T.usable) atomicOr(&S.abort_, (unsigned)kStTableFull);
+            if (pops > pop_limit) atomicOr(&S.abort_, (unsigned)kStTimeout);
           }
         }
-      }
-      __syncthreads();
-      // the messages are read: the buffer takes the next round's
-      if (threadIdx.x < kTeamWarps) S.inbox_n[pin * kTeamWarps + threadIdx.x] = 0u;
-      // this warp's blocks, last queued first
-      while (!skip) {
-        unsigned ab = 0;
-        if (lane == 0) ab = *(volatile unsigned*)&S.abort_;
-        if (__shfl_sync(kFull, ab, 0)) break;
-        const unsigned t = W.top;
-        if (t == 0u) break;
-        const uint32_t slot =
-            t - 1u < (unsigned)kWStack ? W.stack[t - 1u] : ldcg32(&T.spill[t - 1u]);
-        __syncwarp();
-        if (lane == 0) W.top = t - 1u;
-        __syncwarp();
-        w_block(W, T, slot, lane, A, &tm);
-        ++pops;
-        if (lane == 0) {
-          if (W.used > T.usable) atomicOr(&S.abort_, (unsigned)kStTableFull);
-          if (pops > pop_limit) atomicOr(&S.abort_, (unsigned)kStTimeout);
-        }
+        if (skip || team_drain(S, W, T, tm, tm.post, wid, lane) == 0u) break;
       }
       __syncthreads();
       const bool ab = S.abort_ != 0u;
-      const int more =
-          __syncthreads_or(lane == 0 && S.inbox_n[tm.post * kTeamWarps + wid] != 0u);
+      const int more = __syncthreads_or(lane == 0 && S.inbox_n[tm.post * kTeamWarps + wid] >
+                                                         S.inbox_rd[tm.post * kTeamWarps + wid]);
       if (ab || !more) break;
       if (round + 1 >= kTeamRounds) {
         if (threadIdx.x == 0) atomicOr(&S.abort_, (unsigned)kStTimeout);
@@ -1978,6 +2031,13 @@ tfill_kernel(const PointIn* points, int npoints, const DevLens* lenses, const in
     }
     __syncthreads();
     const uint32_t fin = S.status | S.abort_;
+    // a point given up on may leave messages unread (and its counters
+    // reset): every slot of the team's inboxes reads "unwritten" again
+    if (S.abort_) {
+      uint32_t* all = (uint32_t*)tm.inbox;
+      const size_t nslot = (size_t)2 * kTeamWarps * tm.cap;
+      for (size_t q = threadIdx.x; q < nslot; q += blockDim.x) __stcg(&all[4 * q + 3], 0u);
+    }
     if (threadIdx.x == 0) {
       PointOut o = out[p];
       o.count = S.count;
@@ -2014,6 +2074,8 @@ void tscratch_init(WScratch* s, void* base, int teams, int cap_log2, unsigned in
   const size_t wb = wscratch_bytes(teams * kTeamWarps, cap_log2);
   s->inbox = (uint4*)(((uintptr_t)base + wb + 255) / 256 * 256);
   s->inbox_cap = inbox_cap;
+  // every message slot reads "unwritten" (bits 0) until a sender writes it
+  cudaMemsetAsync(s->inbox, 0, (size_t)teams * 2 * kTeamWarps * inbox_cap * sizeof(uint4), st);
 }
 
 void launch_tfill(const PointIn* d_points, int npoints, const DevLens* d_lenses,
