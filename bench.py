@@ -401,12 +401,12 @@ def max_over_ranks(value, dist, device):
     return float(t.item())
 
 
-def parity_vs_fixture(cnt, n, ncurves, seed, rank):
+def parity_vs_fixture(cnt, n, ncurves, seed, rank, ppr=500):
     """Ray counts of the benchmark's first curves against the reference's own
     counts for them (tests/golden/bench_seed2024.npz, strict IEEE build of
     the reference, 8 curves of seed 2024)."""
     path = os.path.join(ROOT, "tests", "golden", "bench_seed2024.npz")
-    if rank != 0 or seed != 2024 or not os.path.exists(path):
+    if rank != 0 or seed != 2024 or ppr != 500 or not os.path.exists(path):
         return None
     z = np.load(path)
     if int(z["n"]) != n:
@@ -460,6 +460,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--curves", type=int, default=152, help="light curves per step per GPU")
     ap.add_argument("--points", type=int, default=5000)
+    ap.add_argument("--ppr", type=int, default=500, help="rays per source radius")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--chain", type=int, default=0,
                     help="warm-start chain: 0 = one per curve (the reference's, exact), "
@@ -508,13 +509,13 @@ def main():
     from triplelens_gb300 import workloads
     # weak scaling: every rank its own curves
     lenses, trajs, n = workloads.config2(rank_seed(args.seed, rank), n_curves=args.curves,
-                                        n_points=args.points)
+                                        n_points=args.points, ppr=args.ppr)
     chain_desc = ("one warm-start chain per curve (the reference's order)" if args.chain <= 0
                   else "warm-start chain restarted every %d points" % args.chain)
     config = {"workload": "config2: %d random triple lenses x %d-point curves, rho=1e-3, "
-                          "500 rays/radius, linear LD v=0.5" % (args.curves, n),
+                          "%d rays/radius, linear LD v=0.5" % (args.curves, n, args.ppr),
               "curves_per_gpu": args.curves, "points_per_curve": n + 1, "rho": 1e-3,
-              "rays_per_radius": 500, "ld_v": 0.5, "seed": args.seed, "chain": chain_desc,
+              "rays_per_radius": args.ppr, "ld_v": 0.5, "seed": args.seed, "chain": chain_desc,
               "l2": "flushed between steps (256 MiB write)",
               "overlap": ("exact chain in 8 segments, each segment's fill overlapped with the "
                           "next segment's chain" if args.chain <= 0 else "none"),
@@ -666,7 +667,7 @@ def main():
                 "seeds_ms": e0.elapsed_time(e1),
                 "points_per_s": npts / (e0.elapsed_time(e2) / 1e3),
                 "count_mismatches_vs_exact": int(np.sum(fcnt != cnt)),
-                "parity": parity_vs_fixture(fcnt, n, len(lenses), args.seed, rank)}
+                "parity": parity_vs_fixture(fcnt, n, len(lenses), args.seed, rank, args.ppr)}
         del bf
         leg("chunked-chain leg")
 
@@ -725,7 +726,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded random lenses and trajectories)", "config": config,
         "e2e": e2e,
-        "parity": parity_vs_fixture(cnt, n, len(lenses), args.seed, rank),
+        "parity": parity_vs_fixture(cnt, n, len(lenses), args.seed, rank, args.ppr),
         "incomplete_points": incomplete,
         "status_counts": status_counts(st),
         "seeds_ms_per_step": (seq_ms if pipelined else ms_step) - fill_ms / args.steps,

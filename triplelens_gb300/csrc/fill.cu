@@ -340,13 +340,13 @@ __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
 // A ray at pixel offset delta from the centre then maps in FP32 to
 //   s = D0 + delta - sum_{n<=K} c_n eps^n,      r^2 = |s|^2,
 // every quantity of size rho, so FP32 rounding is relative to rho, not to
-// the coordinates.  K (<= 8) is the smallest order whose tail bound
+// the coordinates.  The expansion is used where some order K <= 4 has a tail
+// bound
 //   T_K = sum_i m_i |u_i| q_i^(K+1) / (1 - q_i),  q_i = |u_i| |delta|max
-// is below u*rho/2; where no K qualifies, the exact difference form
+// below u*rho/2, and then always with K = 4 terms (one compiled variant);
+// where no K qualifies, the exact difference form
 //   s = D0 + delta + sum_i m_i conj(delta / ((W_i + delta) W_i))
 // is used in FP32, and where a lens lies inside the super-tile, FP64.
-// K is rounded up to 2 or 4 (two compiled variants); super-tiles that need
-// more terms use the exact difference form in FP32.
 // From the magnitudes of the terms the super-tile also gets an error bound E
 // on s and a band B = 4 rho E + 4 E^2 + 4 u rho^2 on r^2: a ray with
 // |r^2 - rho^2| <= B is classified by the exact FP64 map (irs_exact), so the
@@ -445,9 +445,10 @@ __device__ __noinline__ void supertile_values(const Ctx& c, int sxi, int syi, in
     for (int k = 1; k <= 4; k++)
       if (tk[k] <= 0.5 * u * c.rho) { K = k; break; }
   }
-  // two compiled orders keep the kernel's code and registers small: round K
-  // up to 2 or 4 (more terms only shrink the tail)
-  if (K > 0) K = K <= 2 ? 2 : 4;
+  // one compiled order keeps the kernels' hot code small (instruction fetch
+  // is their largest stall): every expansion uses 4 terms (more terms only
+  // shrink the tail; the bound E below is the one of 4 terms)
+  if (K > 0) K = 4;
   if (K > 0) {
     double sc = 0.0, dp = dmax;
     for (int n = 0; n < K; n++) {
@@ -747,7 +748,7 @@ __device__ __noinline__ float weight_again(const Ctx& c, const SuperTile& st, bo
   const float bx = st.d0x + dx;
   float r2;
   if (st.mode == kModeTaylor) {
-    r2 = st.K <= 2 ? taylor_r2<2>(st, dx, bx, dy) : taylor_r2<4>(st, dx, bx, dy);
+    r2 = taylor_r2<4>(st, dx, bx, dy);
   } else {
     r2 = exact32_r2(c, st, dx, bx, dy);
   }
@@ -787,8 +788,7 @@ __device__ __forceinline__ float block_weights(const Ctx& c, const SuperTile& st
                                                int bx, int by, int lane, uint32_t f,
                                                unsigned* nre) {
   if (split && st.mode == kModeTaylor)
-    return st.K <= 2 ? partial_weights<2>(c, st, bx, by, lane, f, nre)
-                     : partial_weights<4>(c, st, bx, by, lane, f, nre);
+    return partial_weights<4>(c, st, bx, by, lane, f, nre);
   if (split && st.mode == kModeExact32) return partial_weights<0>(c, st, bx, by, lane, f, nre);
   float acc = 0.f;
   unsigned re = 0;
@@ -896,7 +896,6 @@ __device__ void process_block(Shared& S, const Table& T, int slot, int lane, War
         const SuperTile stc = wst.st;  // by value: the coefficients stay in registers
         const int K = stc.mode == kModeTaylor ? stc.K : 0;
         if (K == 0) h_row = classify_block<BH, 0>(c, stc, bx, by, lane, &wall, &nr, &n64);
-        else if (K <= 2) h_row = classify_block<BH, 2>(c, stc, bx, by, lane, &wall, &nr, &n64);
         else h_row = classify_block<BH, 4>(c, stc, bx, by, lane, &wall, &nr, &n64);
       } else {
         h_row = classify_block_fp64<BH>(c, bx, by, lane, &wall, &nr, &n64);
@@ -1489,7 +1488,6 @@ __device__ __noinline__ void w_block(WarpSh& W, const WTable& T, uint32_t slot, 
       const SuperTile stc = W.st[sti];   // by value: the coefficients stay in registers
       const int K = stc.mode == kModeTaylor ? stc.K : 0;
       if (K == 0) h_row = classify_block<32, 0>(c, stc, bx, by, lane, &wall, &nr, &n64);
-      else if (K <= 2) h_row = classify_block<32, 2>(c, stc, bx, by, lane, &wall, &nr, &n64);
       else h_row = classify_block<32, 4>(c, stc, bx, by, lane, &wall, &nr, &n64);
     } else {
       h_row = classify_block_fp64<32>(c, bx, by, lane, &wall, &nr, &n64);
