@@ -747,10 +747,12 @@ def main():
                  "status_or": int(np.bitwise_or.reduce(st))},
         "fast_chain": fast,
         "clocks": clocks,
-        # per step: caustic scan, point prep and the chain kernel (or the scan
-        # and the chunked seeds kernel), 3 ordering kernels, the warp fill, and
-        # three CTA-fill levels for its overflow (collect + fill each)
-        "gpu_launches": (13 if args.chain <= 0 else 12) * args.steps,
+        # per overlapped step: caustic scan, point prep, chain reset, 8 chain
+        # segments with 8 warp fills, the team fill and two CTA-fill levels
+        # (collect + fill each) = 25; per sequential step: scan, prep and chain
+        # (or scan and chunked seeds), 3 ordering kernels, the warp fill, the
+        # team fill and two CTA levels (collect + fill each) = 13 (12)
+        "gpu_launches": (25 if pipelined else (13 if args.chain <= 0 else 12)) * args.steps,
     }
     if rank == 0 and not args.no_noalloc:
         line["noalloc"] = noalloc_leg(lenses[0], trajs[0], n)
