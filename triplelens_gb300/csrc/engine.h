@@ -313,6 +313,7 @@ struct Pipeline {
   int nseg;
   PointPrep* prep;
   RootChain* chains;
+  bool reset_chains = true;   // false: chains hold each curve's state already (objects)
 };
 
 }  // namespace tl

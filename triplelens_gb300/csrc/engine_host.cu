@@ -370,7 +370,7 @@ void Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode
   }
   fill_after(st);
   launch_seeds_prep(P.scan, P.nscan, R.trajs, P.lenses, P.ca, R.trials, P.prep, st);
-  launch_chain_reset(R.trajs, P.ntraj, P.lenses, P.chains, st);
+  if (P.reset_chains) launch_chain_reset(R.trajs, P.ntraj, P.lenses, P.chains, st);
   WScratch w = ws_;
   w.wthr = wfill_thr_;
   w.dump = R.dump;

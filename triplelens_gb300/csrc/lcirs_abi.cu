@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,6 +46,7 @@ struct LightCurveIRS::Impl {
   tl::RunBufs bufs;
   tl::DevBuf specbuf, ampbuf;
   bool failed = false;
+  bool fresh = true;        // no get_lc_irs yet
   bool ck(cudaError_t e) {
     if (e != cudaSuccess) {
       fprintf(stderr, "liblcirs: CUDA error %s\n", cudaGetErrorString(e));
@@ -56,6 +58,10 @@ struct LightCurveIRS::Impl {
 };
 
 namespace {
+
+// objects that have not run get_lc_irs yet: while there are any, a batch
+// waits longer for callers (they are likely on their way)
+std::atomic<int> g_fresh{0};
 
 void setup_object(LightCurveIRS* o) {
   tl::Engine& E = tl::Engine::get();
@@ -111,10 +117,12 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
   lcVec.assign(lcLength, 0.0);
   impl->lcFull.assign((size_t)lcLength + 1, 0.0);
   setup_object(this);
+  g_fresh.fetch_add(1);   // until its first get_lc_irs (batching window)
 }
 
 LightCurveIRS::~LightCurveIRS() {
   tl::Engine::get().trace("delete object");
+  if (impl && impl->fresh) g_fresh.fetch_sub(1);
   if (impl) {
     // stream-ordered releases: no wait for work on other streams
     cudaStream_t st = impl->st;
@@ -244,11 +252,12 @@ void absorb_results(LightCurveIRS* o, std::complex<double> s, std::complex<doubl
 // their own launches from different host threads mostly wait for each
 // other.  Instead, a call queues its request; the first caller that finds no
 // batch running becomes the leader, waits until requests stop arriving (a
-// gap of 3 ms, at most 100 ms), and runs every queued request with its own
-// chain and precision settings as one batch: one seeds launch (a chain per
-// curve) and one fill, on the batcher's stream.  Every caller then finds its
-// results in its object, exactly as a lone call would leave them.  A lone
-// caller pays the 3 ms window once.
+// gap of 3 ms, 15 ms while objects exist that have not called yet; at most
+// 300 ms), and runs every queued request with its chain and precision
+// settings as one batch: the seeds (a chain per curve; the exact chain in
+// segments overlapped with the fill) and the fill, on the batcher's stream.
+// Every caller then finds its results in its object, exactly as a lone call
+// would leave them.  A lone caller pays the 3 ms window once.
 // ---------------------------------------------------------------------------
 struct Request {
   LightCurveIRS* obj;
@@ -266,7 +275,7 @@ struct Batcher {
   uint64_t arrivals = 0;
   cudaStream_t st = nullptr;
   tl::RunBufs bufs;
-  tl::DevBuf lenses, ca, chains;
+  tl::DevBuf lenses, ca, chains, segjobs, seglist, segn;
   std::vector<tl::PointOut> hout;
   std::vector<int32_t> hseeds;
 };
@@ -277,6 +286,10 @@ Batcher& batcher() {
 }
 
 // Runs one batch of requests that share chain mode and precision.
+// segments of the exact chain in a batch (each segment's fill overlaps the
+// next segment's chain)
+constexpr int kBatchSegments = 8;
+
 void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
   tl::Engine& E = tl::Engine::get();
   if (!B.st) cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking);
@@ -325,15 +338,64 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
   ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                      cudaMemcpyHostToDevice, B.st));
   if (chain <= 0) {
+    // the exact chain in segments, each segment's fill beside the next
+    // segment's chain; every curve continues from its object's chain state
     ck(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
                        cudaMemcpyHostToDevice, B.st));
-    tl::launch_seeds_exact(R.scan_jobs, (int)scan.size(), R.jobs, (int)jobs.size(), R.trajs, dl,
-                           dca, R.points, R.seeds, R.out, R.trials, R.prep, dch, B.st);
+    const int S = kBatchSegments;
+    std::vector<tl::SeedJob> sj;
+    std::vector<int32_t> sl;
+    std::vector<unsigned> sn(S, 0);
+    std::vector<int> segoff(S + 1, 0), segjob0(S + 1, 0);
+    for (int s = 0; s < S; s++) {
+      segjob0[s] = (int)sj.size();
+      segoff[s] = (int)sl.size();
+      for (int i = 0; i < k; i++) {
+        const long np = (long)trajs[i].n + 1;
+        const long len = (np + S - 1) / S;
+        const long first = (long)s * len;
+        const long cnt = std::min(len, np - first);
+        if (cnt <= 0) continue;
+        tl::SeedJob j;
+        j.traj = i;
+        j.first = (int32_t)first;
+        j.count = (int32_t)cnt;
+        j.chain = i;
+        sj.push_back(j);
+        for (long q = 0; q < cnt; q++) sl.push_back((int32_t)(base[i] + (size_t)(first + q)));
+      }
+      sn[s] = (unsigned)(sl.size() - (size_t)segoff[s]);
+    }
+    segjob0[S] = (int)sj.size();
+    segoff[S] = (int)sl.size();
+    auto* dsj = (tl::SeedJob*)B.segjobs.need(sizeof(tl::SeedJob) * sj.size(), B.st);
+    auto* dsl = (int32_t*)B.seglist.need(sizeof(int32_t) * sl.size(), B.st);
+    auto* dsn = (unsigned*)B.segn.need(sizeof(unsigned) * S, B.st);
+    ck(cudaMemcpyAsync(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(), cudaMemcpyHostToDevice,
+                       B.st));
+    ck(cudaMemcpyAsync(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
+                       B.st));
+    ck(cudaMemcpyAsync(dsn, sn.data(), sizeof(unsigned) * S, cudaMemcpyHostToDevice, B.st));
+    tl::Pipeline P;
+    P.lenses = dl;
+    P.ca = dca;
+    P.scan = R.scan_jobs;
+    P.nscan = (int)scan.size();
+    P.ntraj = k;
+    P.segjobs = dsj;
+    P.segjob0 = segjob0.data();
+    P.seglist = dsl;
+    P.segoff = segoff.data();
+    P.segn = dsn;
+    P.nseg = S;
+    P.prep = R.prep;
+    P.chains = dch;
+    P.reset_chains = false;
+    std::lock_guard<std::mutex> g(E.mu);
+    E.pipeline_exact(R, total, P, precision, B.st);
   } else {
     tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, dl, dca, R.points, R.seeds, R.out,
                      R.trials, dch, B.st);
-  }
-  {
     std::lock_guard<std::mutex> g(E.mu);
     E.fill_on(R, total, dl, precision, B.st);
   }
@@ -376,12 +438,15 @@ void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
   while (!r.done) {
     if (!B.running) {
       B.running = true;
+      // gather callers: until a quiet gap of 3 ms (15 ms while objects that
+      // have not called yet exist), at most 300 ms
       const auto t0 = std::chrono::steady_clock::now();
       uint64_t seen = B.arrivals;
       for (;;) {
-        B.cv.wait_for(lk, std::chrono::milliseconds(3));
+        const int gap = g_fresh.load() > 0 ? 15 : 3;
+        B.cv.wait_for(lk, std::chrono::milliseconds(gap));
         if (B.arrivals == seen ||
-            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(100))
+            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(300))
           break;
         seen = B.arrivals;
       }
@@ -539,6 +604,10 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
 }
 
 void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
+  if (impl->fresh) {
+    impl->fresh = false;
+    g_fresh.fetch_sub(1);
+  }
   if (amoebaPrintOut_) {
     printOutLCParameters();
     runFill(s, e, nullptr, nullptr);   // the amoeba dump needs the object's own run
