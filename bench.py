@@ -212,7 +212,7 @@ def config4_leg(seed, curves, reps):
     b.set_lenses(lenses)
     npts = b.set_trajectories(trajs, np.arange(curves), np.full(curves, n))
     t0 = time.perf_counter()
-    chosen, times = b.autotune(sample_points=min(npts, 32768))
+    chosen, times = b.autotune(sample_points=0)   # every point: the largest decide
     t_tune = time.perf_counter() - t0
     stream = torch.cuda.Stream()
     b.graph_capture()

@@ -86,7 +86,7 @@ long tlb_point_lc(tl_batch* b, double* amp);
  * 32 x 32 rays): one warp per point up to 7000, 3000 or 1500 blocks and a
  * team of 8 warps per larger point; one warp up to 7000 and the CTA fill for
  * larger points; the CTA fill alone.  Keeps the fastest for later runs of the
- * process.  chosen3 = {warp-fill threshold in blocks (0: CTA fill alone),
+ * process (the first, the default, unless another is 5 % faster).  chosen3 = {warp-fill threshold in blocks (0: CTA fill alone),
  * 1 if the team fill takes the larger points, points timed}; times_ms (5
  * floats, may be NULL) the fill times in that order.  Results do not depend
  * on the choice (the filled sets are exact). */
