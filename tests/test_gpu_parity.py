@@ -105,6 +105,35 @@ def test_fill_from_oracle_seeds_is_exact(product_lib, oracle_lib, precision):
         assert abs(amps[p] - a) <= tol * a, p
 
 
+def test_fill_from_seeds_clamps_seed_counts(product_lib):
+    """lcirs_fill_from_seeds takes seed counts as the caller gives them: a
+    negative count fills nothing, a count above 64 uses the 64 stored pixels
+    (include/lcirs.h); neither reads past the seed array."""
+    lens, traj, n = workloads.config1()
+    lens = lens.copy()
+    lens[6] = 0.5
+    lc = _lc(product_lib, lens, n, 1)
+    lc.get_lc_irs(*traj)
+    counts = lc.counts()
+    seeds, cnt = lc.seeds()
+    # slots past a point's count repeat its first seed pixel: all 64 stored
+    # pixels seed the same components as the first cnt
+    full = np.array(seeds, dtype=np.int32, copy=True)
+    for i, c in enumerate(cnt):
+        if 0 < c < 64:
+            full[i, c:] = full[i, 0]
+    lc.fill_from_seeds(*traj, full, np.full(n + 1, 1000, np.int32))
+    c_big, a_big = lc.counts(), lc.lc_full()
+    lc.fill_from_seeds(*traj, full, np.full(n + 1, 64, np.int32))
+    c_64, a_64 = lc.counts(), lc.lc_full()
+    assert np.array_equal(c_big, c_64)
+    has = np.asarray(cnt) > 0
+    assert np.array_equal(c_64[has], counts[has])
+    assert np.max(np.abs(a_big[has] - a_64[has]) / a_64[has]) < LD_RTOL_SPLIT
+    lc.fill_from_seeds(*traj, full, np.full(n + 1, -1, np.int32))
+    assert np.all(lc.counts() == 0) and np.all(lc.lc_full() == 0.0)
+
+
 def test_amoeba_dump_matches_reference(product_lib, golden_c1, tmp_path):
     lens, traj, n = workloads.config1()
     lens = lens.copy()
