@@ -196,6 +196,20 @@ def hbm_view(traffic_bytes, fill_s, peaks):
             "peak_source": "MEASURED_PEAKS hbm_gbs" if peaks.get("hbm_gbs") else "fallback"}
 
 
+def mufu_view(evaluated_rays, fill_s, sm_mhz, sms):
+    """The fill's special-function work as a rate against the nominal MUFU
+    rate (16 operations per clock per SM): the split map has no divisions,
+    and each evaluated ray takes one square root (its limb-darkening
+    weight)."""
+    if not evaluated_rays or not fill_s or fill_s <= 0 or not sm_mhz or not sms:
+        return None
+    achieved = float(evaluated_rays) / fill_s / 1e12
+    peak = 16.0 * sms * sm_mhz * 1e6 / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "Tops/s", "frac": achieved / peak,
+            "ops_per_ray": 1, "peak_source": "16 MUFU ops/clock/SM x %d SMs x %.0f MHz (nominal)"
+                                            % (sms, sm_mhz)}
+
+
 # ---------------------------------------------------------------------------
 def config4_leg(seed, curves, reps):
     """Config 4 (sub-sample): `curves` light curves of 2000 points, each its
@@ -740,7 +754,8 @@ def main():
                      "peak_source": "2 x 128 FP32 lanes x %d SMs x sm_max_mhz %.0f (MEASURED_PEAKS)"
                                     % (sms, sm_max),
                      "fill_ms_per_step": fill_ms / args.steps,
-                     "hbm_view": hbm_view(traffic, fill_s, peaks)},
+                     "hbm_view": hbm_view(traffic, fill_s, peaks),
+                     "mufu_view": mufu_view(stats[0], fill_s, sm_max, sms)},
         "rays": {"accepted_per_step": int(stats[3]), "evaluated_per_step": int(stats[0]),
                  "fp64_per_step": int(stats[1]), "tiles_per_step": int(stats[2]),
                  "accepted_per_s": float(stats[3]) * world / (ms_step / 1e3),

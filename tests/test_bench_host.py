@@ -18,6 +18,18 @@ def test_hbm_view():
     assert bench.hbm_view(1.0, 0.0, {}) is None
 
 
+def test_mufu_view():
+    import bench
+    v = bench.mufu_view(1.0e12, 4.0, 2070.0, 152)
+    assert abs(v["achieved"] - 0.25) < 1e-12
+    assert abs(v["peak"] - 16 * 152 * 2.07e9 / 1e12) < 1e-9
+    assert abs(v["frac"] - 0.25 / v["peak"]) < 1e-12
+    assert bench.mufu_view(0, 4.0, 2070.0, 152) is None
+    assert bench.mufu_view(1.0e12, 0.0, 2070.0, 152) is None
+    import numpy as np
+    assert bench.mufu_view(np.uint64(10 ** 12), 4.0, 2070.0, 152)["achieved"] > 0
+
+
 def test_reference_arm_prints_one_json_line():
     """`bench.py --impl reference` (the oracle on the host cores) prints the
     contract's line with impl, cpu_baseline and e2e."""
