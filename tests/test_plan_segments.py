@@ -1,0 +1,84 @@
+"""Host planning of the exact chain in segments (triplelens_gb300/csrc/plan.h)
+without a GPU: the header compiles alone with g++, and on random sets of
+curve lengths (including curves shorter than the number of segments) every
+point is listed exactly once, each curve's segments are consecutive shares
+in order with the curve as their chain, and the counts and offsets agree.
+The seeds of a segmented chain equal one unbroken chain only if these hold
+(the GPU tests check the seeds themselves)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+PROGRAM = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <set>
+#include "plan.h"
+
+struct Job { int32_t traj, first, count, chain; };
+
+int main() {
+  unsigned seed = 12345u;
+  auto rnd = [&]() { seed = seed * 1103515245u + 12345u; return (seed >> 8) & 0xffffff; };
+  for (int trial = 0; trial < 300; trial++) {
+    const int nseg = 1 + (int)(rnd() % 12);
+    const int nc = 1 + (int)(rnd() % 20);
+    std::vector<int64_t> base(nc);
+    std::vector<uint32_t> n(nc);
+    int64_t b = 0;
+    for (int i = 0; i < nc; i++) {
+      n[i] = (uint32_t)(rnd() % 60);          // 1..60 points, often fewer than nseg
+      base[i] = b;
+      b += (int64_t)n[i] + 1;
+    }
+    std::vector<Job> jobs;
+    std::vector<int32_t> list;
+    std::vector<unsigned> count;
+    std::vector<int> job0, off;
+    tl::plan_segments(nseg, nc, base.data(), n.data(), &jobs, &list, &count, &job0, &off);
+    if ((int64_t)list.size() != b) { printf("FAIL total %zu %lld\n", list.size(), (long long)b); return 1; }
+    std::set<int32_t> seen(list.begin(), list.end());
+    if ((int64_t)seen.size() != b) { printf("FAIL duplicates\n"); return 1; }
+    if (job0[0] != 0 || off[0] != 0 || job0[nseg] != (int)jobs.size() || off[nseg] != (int)list.size()) {
+      printf("FAIL ends\n"); return 1;
+    }
+    std::vector<long> next(nc, 0);           // next point expected per curve
+    for (int s = 0; s < nseg; s++) {
+      if (count[s] != (unsigned)(off[s + 1] - off[s])) { printf("FAIL count\n"); return 1; }
+      int pos = off[s], prev = -1;
+      for (int q = job0[s]; q < job0[s + 1]; q++) {
+        const Job& j = jobs[q];
+        if (j.chain != j.traj || j.traj <= prev || j.count <= 0) { printf("FAIL job\n"); return 1; }
+        prev = j.traj;
+        if (j.first != next[j.traj]) { printf("FAIL order\n"); return 1; }
+        for (int k = 0; k < j.count; k++)
+          if (list[pos++] != (int32_t)(base[j.traj] + j.first + k)) { printf("FAIL list\n"); return 1; }
+        next[j.traj] = (long)j.first + j.count;
+      }
+      if (pos != off[s + 1]) { printf("FAIL offsets\n"); return 1; }
+    }
+    for (int i = 0; i < nc; i++)
+      if (next[i] != (long)n[i] + 1) { printf("FAIL coverage\n"); return 1; }
+  }
+  printf("OK\n");
+  return 0;
+}
+"""
+
+
+def test_plan_segments_covers_every_point_once_in_chain_order(tmp_path):
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    src = tmp_path / "plan_test.cc"
+    src.write_text(PROGRAM)
+    exe = tmp_path / "plan_test"
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "triplelens_gb300", "csrc"),
+                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr

@@ -10,6 +10,7 @@
 #include "batch_internal.h"
 #include "engine.h"
 #include "engine_host.h"
+#include "plan.h"
 #include "tl_batch.h"
 
 using tl::cx;
@@ -132,30 +133,14 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
     const int S = kSegments;
     std::vector<tl::SeedJob> sj;
     std::vector<int32_t> sl;
-    std::vector<unsigned> sn(S, 0);
-    b->segoff.assign(S + 1, 0);
-    b->segjob0.assign(S + 1, 0);
-    for (int s = 0; s < S; s++) {
-      b->segjob0[s] = (int)sj.size();
-      b->segoff[s] = (int)sl.size();
-      for (int i = 0; i < ntraj; i++) {
-        const long np = (long)b->htraj[i].n + 1;
-        const long len = (np + S - 1) / S;
-        const long first = (long)s * len;
-        const long cnt = std::min(len, np - first);
-        if (cnt <= 0) continue;
-        tl::SeedJob j;
-        j.traj = i;
-        j.first = (int32_t)first;
-        j.count = (int32_t)cnt;
-        j.chain = i;   // the curve's chain, carried from segment to segment
-        sj.push_back(j);
-        for (long q = 0; q < cnt; q++) sl.push_back((int32_t)(b->htraj[i].point_base + first + q));
-      }
-      sn[s] = (unsigned)(sl.size() - b->segoff[s]);
+    std::vector<unsigned> sn;
+    std::vector<int64_t> pb(ntraj);
+    std::vector<uint32_t> nn(ntraj);
+    for (int i = 0; i < ntraj; i++) {
+      pb[i] = b->htraj[i].point_base;
+      nn[i] = b->htraj[i].n;
     }
-    b->segjob0[S] = (int)sj.size();
-    b->segoff[S] = (int)sl.size();
+    tl::plan_segments(S, ntraj, pb.data(), nn.data(), &sj, &sl, &sn, &b->segjob0, &b->segoff);
     void* dsj = b->segjobs.need(sizeof(tl::SeedJob) * sj.size());
     void* dsl = b->seglist.need(sizeof(int32_t) * sl.size());
     void* dsn = b->segn.need(sizeof(unsigned) * S);

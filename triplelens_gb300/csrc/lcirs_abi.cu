@@ -24,6 +24,7 @@
 
 #include "engine.h"
 #include "engine_host.h"
+#include "plan.h"
 #include "lcirs.hpp"
 
 using tl::cx;
@@ -345,29 +346,15 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
     const int S = kBatchSegments;
     std::vector<tl::SeedJob> sj;
     std::vector<int32_t> sl;
-    std::vector<unsigned> sn(S, 0);
-    std::vector<int> segoff(S + 1, 0), segjob0(S + 1, 0);
-    for (int s = 0; s < S; s++) {
-      segjob0[s] = (int)sj.size();
-      segoff[s] = (int)sl.size();
-      for (int i = 0; i < k; i++) {
-        const long np = (long)trajs[i].n + 1;
-        const long len = (np + S - 1) / S;
-        const long first = (long)s * len;
-        const long cnt = std::min(len, np - first);
-        if (cnt <= 0) continue;
-        tl::SeedJob j;
-        j.traj = i;
-        j.first = (int32_t)first;
-        j.count = (int32_t)cnt;
-        j.chain = i;
-        sj.push_back(j);
-        for (long q = 0; q < cnt; q++) sl.push_back((int32_t)(base[i] + (size_t)(first + q)));
-      }
-      sn[s] = (unsigned)(sl.size() - (size_t)segoff[s]);
+    std::vector<unsigned> sn;
+    std::vector<int> segoff, segjob0;
+    std::vector<int64_t> pb(k);
+    std::vector<uint32_t> nn(k);
+    for (int i = 0; i < k; i++) {
+      pb[i] = (int64_t)base[i];
+      nn[i] = trajs[i].n;
     }
-    segjob0[S] = (int)sj.size();
-    segoff[S] = (int)sl.size();
+    tl::plan_segments(S, k, pb.data(), nn.data(), &sj, &sl, &sn, &segjob0, &segoff);
     auto* dsj = (tl::SeedJob*)B.segjobs.need(sizeof(tl::SeedJob) * sj.size(), B.st);
     auto* dsl = (int32_t*)B.seglist.need(sizeof(int32_t) * sl.size(), B.st);
     auto* dsn = (unsigned*)B.segn.need(sizeof(unsigned) * S, B.st);

@@ -1,0 +1,56 @@
+// plan.h - host-side planning of the exact warm-start chain in segments
+// (no CUDA; included by the batched API and the object batcher, and compiled
+// alone by the CPU tests).
+//
+// Every curve's n+1 points are cut into nseg consecutive shares of
+// ceil((n+1)/nseg) points (the last shares of a short curve may be empty).
+// Segment s holds one job per curve that has points in it, in curve order,
+// with the curve's index as its chain (the chain state goes from segment to
+// segment), and lists those points' flat indices in the same order.
+#pragma once
+
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+namespace tl {
+
+// Job: any type with int32_t fields traj, first, count, chain (SeedJob).
+// jobs/list are filled in segment order; job0[s] and off[s] (nseg + 1
+// entries) are where segment s starts in jobs and list; count[s] = the
+// number of points of segment s.
+template <class Job>
+void plan_segments(int nseg, int ncurves, const int64_t* point_base, const uint32_t* n,
+                   std::vector<Job>* jobs, std::vector<int32_t>* list,
+                   std::vector<unsigned>* count, std::vector<int>* job0,
+                   std::vector<int>* off) {
+  jobs->clear();
+  list->clear();
+  count->assign((size_t)nseg, 0u);
+  job0->assign((size_t)nseg + 1, 0);
+  off->assign((size_t)nseg + 1, 0);
+  for (int s = 0; s < nseg; s++) {
+    (*job0)[s] = (int)jobs->size();
+    (*off)[s] = (int)list->size();
+    for (int i = 0; i < ncurves; i++) {
+      const long np = (long)n[i] + 1;
+      const long len = (np + nseg - 1) / nseg;
+      const long first = (long)s * len;
+      const long cnt = std::min(len, np - first);
+      if (cnt <= 0) continue;
+      Job j;
+      j.traj = i;
+      j.first = (int32_t)first;
+      j.count = (int32_t)cnt;
+      j.chain = i;   // the curve's chain, carried from segment to segment
+      jobs->push_back(j);
+      for (long q = 0; q < cnt; q++) list->push_back((int32_t)(point_base[i] + first + q));
+    }
+    (*count)[s] = (unsigned)(list->size() - (size_t)(*off)[s]);
+  }
+  (*job0)[nseg] = (int)jobs->size();
+  (*off)[nseg] = (int)list->size();
+}
+
+}  // namespace tl
