@@ -259,7 +259,10 @@ def config4_leg(seed, curves, reps):
                                            "warp<=7000+cta": float(times[3]),
                                            "cta": float(times[4])},
                          "seconds": round(t_tune, 2)},
-            "status_or": int(np.bitwise_or.reduce(st))}
+            "status_or": int(np.bitwise_or.reduce(st)),
+            # points whose magnification is incomplete (table full or a wait ran out)
+            "incomplete_points": int(((st & 0xC) != 0).sum()),
+            "status_counts": status_counts(st)}
 
 
 def surrogate_leg(seed, train_lenses, eval_lenses):
