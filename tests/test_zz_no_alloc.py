@@ -6,7 +6,8 @@ loops that cannot take cudaFree's device-wide synchronisation): it runs the
 fill kernel with a static 80 MiB scratch array instead of allocated tables.
 Given the same seed pixels and source positions it must give the same ray
 counts (exactly) and magnifications (within the limb-darkening tolerance of
-the other GPU tests) as the allocating fill entry point.  Two calls in a row
+the other GPU tests) as the allocating fill entry point, and on config 1 the
+reference's own counts (tests/golden/config1.npz).  Two calls in a row
 on different lenses and trajectories check that the shared array's leftovers
 from one call do not reach the next; device free memory around the second
 call checks that nothing is allocated.
@@ -80,7 +81,7 @@ def _run_noalloc(fn, lc, xy, seeds, nseeds):
             d_st.cpu().numpy().view(np.uint32), free0, free1)
 
 
-def test_noalloc_matches_fill_from_seeds_twice(product_lib):
+def test_noalloc_matches_fill_from_seeds_twice(product_lib, golden_c1):
     import torch
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -101,6 +102,10 @@ def test_noalloc_matches_fill_from_seeds_twice(product_lib):
         mag, cnt, st, free0, free1 = _run_noalloc(fn, lc, _positions(traj, n), seeds, nseeds)
         assert np.array_equal(st, status), "call %d: status words differ" % k
         assert np.array_equal(cnt, counts), "call %d: ray counts differ" % k
+        if k == 0:
+            # config 1: also the reference's own counts (strict IEEE build;
+            # the counts do not depend on limb darkening)
+            assert np.array_equal(cnt, golden_c1["counts_linear05_strict"])
         assert np.max(np.abs(mag - amps) / amps) < LD_RTOL, "call %d" % k
         if k > 0:
             # the array's address was looked up on the first call: later
