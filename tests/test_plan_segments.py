@@ -4,7 +4,8 @@ curve lengths (including curves shorter than the number of segments) every
 point is listed exactly once, each curve's segments are consecutive shares
 in order with the curve as their chain, and the counts and offsets agree.
 The seeds of a segmented chain equal one unbroken chain only if these hold
-(the GPU tests check the seeds themselves)."""
+(the GPU tests check the seeds themselves).  The same header holds the
+autotuner's choice among its timed candidates, tested here on set timings."""
 import os
 import shutil
 import subprocess
@@ -70,15 +71,53 @@ int main() {
 """
 
 
-def test_plan_segments_covers_every_point_once_in_chain_order(tmp_path):
+PICK = r"""
+#include <cstdio>
+#include "plan.h"
+
+static int fails = 0;
+static void check(const char* what, std::initializer_list<float> t, int want) {
+  std::vector<float> v(t);
+  const int got = tl::pick_candidate(v.data(), (int)v.size(), 0.05f);
+  if (got != want) { printf("FAIL %s: got %d want %d\n", what, got, want); fails++; }
+}
+
+int main() {
+  check("default fastest", {100, 120, 130, 110, 140}, 0);
+  check("within the margin", {100, 96, 99, 97, 98}, 0);
+  check("exactly 5 % faster stays", {100, 95, 120, 120, 120}, 0);
+  check("clearly faster wins", {100, 120, 80, 120, 120}, 2);
+  // the fastest wins, not the first candidate past the margin
+  check("fastest of several", {100, 94, 92, 120, 120}, 2);
+  check("failed default", {-1, 120, 110, 130, 140}, 2);
+  check("failed candidate ignored", {100, -1, 0, 99, 98}, 0);
+  check("nothing ran", {-1, -1, -1, -1, -1}, 0);
+  if (fails) return 1;
+  printf("OK\n");
+  return 0;
+}
+"""
+
+
+def _compile_and_run(tmp_path, name, program):
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("no g++")
-    src = tmp_path / "plan_test.cc"
-    src.write_text(PROGRAM)
-    exe = tmp_path / "plan_test"
+    src = tmp_path / (name + ".cc")
+    src.write_text(program)
+    exe = tmp_path / name
     r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "triplelens_gb300", "csrc"),
                         str(src), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
+
+
+def test_plan_segments_covers_every_point_once_in_chain_order(tmp_path):
+    _compile_and_run(tmp_path, "plan_test", PROGRAM)
+
+
+def test_autotuner_keeps_the_default_unless_the_fastest_beats_it_by_5_percent(tmp_path):
+    """tlb_autotune's choice among its five fill-stage candidates
+    (triplelens_gb300/csrc/batch_abi.cu) through tl::pick_candidate."""
+    _compile_and_run(tmp_path, "pick_test", PICK)

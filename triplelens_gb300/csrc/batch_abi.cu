@@ -293,8 +293,7 @@ int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times
   // threshold (blocks of 32 x 32 rays), then 8 warps per point (team fill)
   // or the CTA fill; {threshold, team} (threshold 0: the CTA fill alone)
   const int cand[5][2] = {{7000, 1}, {3000, 1}, {1500, 1}, {7000, 0}, {0, 0}};
-  float best = 3.0e38f;
-  int best_thr = 7000, best_team = 1;
+  float msk[5];
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -323,18 +322,13 @@ int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times
       }
     }
     if (times_ms) times_ms[k] = ms;
-    // the first candidate (the default) stays unless another is 5 % faster:
-    // timings on a sample vary by a few per cent from run to run
-    const float bar = k == 0 ? ms : best * 0.95f;
-    k++;
-    if (ms > 0.f && (best > 1.0e38f || ms < bar)) {
-      best = ms;
-      best_thr = c[0];
-      best_team = c[1];
-    }
+    msk[k++] = ms;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  // the first candidate (the default) stays unless the fastest beats it by 5 %
+  const int pick = tl::pick_candidate(msk, 5, 0.05f);
+  const int best_thr = cand[pick][0], best_team = cand[pick][1];
   {
     std::lock_guard<std::mutex> g(E.mu);
     E.set_fill_paths(best_thr > 0, best_team != 0, (unsigned)best_thr);

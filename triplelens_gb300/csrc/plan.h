@@ -1,8 +1,8 @@
-// plan.h - host-side planning of the exact warm-start chain in segments
-// (no CUDA; included by the batched API and the object batcher, and compiled
-// alone by the CPU tests).
+// plan.h - host-side planning (no CUDA; included by the batched API and the
+// object batcher, and compiled alone by the CPU tests): the exact warm-start
+// chain in segments, and the autotuner's choice among timed candidates.
 //
-// Every curve's n+1 points are cut into nseg consecutive shares of
+// Segments: every curve's n+1 points are cut into nseg consecutive shares of
 // ceil((n+1)/nseg) points (the last shares of a short curve may be empty).
 // Segment s holds one job per curve that has points in it, in curve order,
 // with the curve's index as its chain (the chain state goes from segment to
@@ -51,6 +51,20 @@ void plan_segments(int nseg, int ncurves, const int64_t* point_base, const uint3
   }
   (*job0)[nseg] = (int)jobs->size();
   (*off)[nseg] = (int)list->size();
+}
+
+// The autotuner's choice: ms[k] is candidate k's time (<= 0: it failed), and
+// candidate 0 is the default.  The fastest candidate wins only if it beats
+// the default by more than `margin` (a fraction): timings on a sample vary
+// by a few per cent from run to run.  A failed default loses to the fastest
+// candidate that ran; if none ran, the default stays.
+inline int pick_candidate(const float* ms, int n, float margin) {
+  int best = -1;
+  for (int k = 0; k < n; k++)
+    if (ms[k] > 0.f && (best < 0 || ms[k] < ms[best])) best = k;
+  if (best < 0) return 0;
+  if (ms[0] > 0.f && ms[best] >= (1.f - margin) * ms[0]) return 0;
+  return best;
 }
 
 }  // namespace tl
