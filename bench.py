@@ -694,14 +694,21 @@ def main():
         with quiet_stdout():
             e2e_objects(lenses, trajs, n, args.chain, threads)          # warm-up pass
             torch.cuda.synchronize()
+            from triplelens_gb300.lcirs import transfer_bytes
+            x0 = transfer_bytes()
             t_e2e, outs = e2e_objects(lenses, trajs, n, args.chain, threads)
+            x1 = transfer_bytes()
         ref_amp = amp.reshape(len(lenses), n + 1)[:, :n]
         rel = float(np.max(np.abs(outs - ref_amp) / ref_amp))
-        # bytes across the host boundary per step (per curve: lens + trajectory
-        # parameters in, n magnifications out)
+        # bytes across the host boundary per step, as the library counts its
+        # own copies (parameters, jobs and point lists in; per-point results
+        # and seeds out); the caller's own buffers hold the parameters and
+        # the n magnifications per curve
         e2e = {"value": npts * world / t_e2e, "unit": UNIT,
-               "h2d_bytes_per_step": len(lenses) * (8 * 8 + 4 * 8),
-               "d2h_bytes_per_step": len(lenses) * n * 8,
+               "h2d_bytes_per_step": x1[0] - x0[0],
+               "d2h_bytes_per_step": x1[1] - x0[1],
+               "caller_bytes_per_step": {"in": len(lenses) * (8 * 8 + 4 * 8),
+                                         "out": len(lenses) * n * 8},
                "path": "lcirs_new/set_limb_darkening/get_lc_irs/copy_lc per curve (reference C "
                        "ABI), %d host threads, lens set-up included" % threads,
                "max_rel_diff_vs_device_run": rel}
@@ -712,11 +719,15 @@ def main():
         cntb = np.zeros(npts, np.uint64)
         stb = np.zeros(npts, np.uint32)
         for it in range(2):
+            x0 = transfer_bytes()
             t0 = time.perf_counter()
             bh.set_lenses(lenses)
             bh.run_host(trajs, np.arange(len(trajs)), np.full(len(trajs), n), ampb, cntb, stb)
             t_b = time.perf_counter() - t0
+            x1 = transfer_bytes()
         e2e["batch_api"] = {"value": npts * world / t_b, "unit": UNIT,
+                            "h2d_bytes_per_step": x1[0] - x0[0],
+                            "d2h_bytes_per_step": x1[1] - x0[1],
                             "path": "tlb_set_lenses + tlb_run_host (host buffers in and out)",
                             "counts_equal_device_run": bool(np.array_equal(cntb, cnt))}
         del bh

@@ -95,6 +95,12 @@ void lcirs_fill_from_seeds(LightCurveIRS* lc, double iniX, double iniY, double f
  * FP64, tiles visited (3 x uint64 totals). */
 void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3);
 
+/* Bytes the library has copied host -> device and device -> host for the
+ * lcirs_* and tlb_* calls of this process (2 x uint64 totals since load):
+ * the parameters, point lists and jobs going in; the per-point results and
+ * seeds coming back.  Additive, for end-to-end accounting; no GPU work. */
+void lcirs_copy_transfer_bytes(uint64_t* out2);
+
 /* Ray-map precision: 0 = every ray in FP64 (irsSIMD order); 1 = FP32
  * tile-relative map with an FP64 guard band at the limb (default). */
 void lcirs_set_precision(LightCurveIRS* lc, int mode);

@@ -110,3 +110,19 @@ def test_static_noalloc_scratch_lives_in_liblcirs_only(product_lib):
     lccuda = ctypes.CDLL(os.path.join(os.path.dirname(product_lib), "liblccuda.so"))
     assert hasattr(lcirs, "lcirs_fill_device_noalloc")
     assert not hasattr(lccuda, "lcirs_fill_device_noalloc")
+
+
+def test_transfer_byte_counters_read_without_a_gpu(product_lib):
+    """lcirs_copy_transfer_bytes reports the library's own host<->device copy
+    totals (include/lcirs.h): readable with no GPU work, zero before any
+    copy, and tolerant of a null output pointer."""
+    from triplelens_gb300.lcirs import transfer_bytes
+    lib = ctypes.CDLL(product_lib)
+    lib.lcirs_copy_transfer_bytes.argtypes = [ctypes.c_void_p]
+    lib.lcirs_copy_transfer_bytes.restype = None
+    lib.lcirs_copy_transfer_bytes(None)
+    h2d, d2h = transfer_bytes(product_lib)
+    assert h2d >= 0 and d2h >= 0
+    import torch
+    if not torch.cuda.is_available():
+        assert (h2d, d2h) == (0, 0)

@@ -66,13 +66,13 @@ int tlb_set_lenses(tl_batch* b, int nlens, const double* p8) {
   void* dcc = b->cc.need(sizeof(cx) * tl::kBranches * tl::kCCLen * nlens);
   void* dca = b->ca.need(sizeof(cx) * tl::kBranches * tl::kCCLen * nlens);
   if (!ds || !dl || !dcc || !dca) return -2;
-  if (!E.check(cudaMemcpyAsync(ds, specs.data(), sizeof(tl::LensSpec) * nlens,
+  if (!E.check(tl::copy_async(ds, specs.data(), sizeof(tl::LensSpec) * nlens,
                                cudaMemcpyHostToDevice, E.stream)))
     return -2;
   tl::launch_lens_setup((const tl::LensSpec*)ds, nlens, (tl::DevLens*)dl, (cx*)dcc, (cx*)dca,
                         E.stream);
   b->hlens.resize(nlens);
-  E.check(cudaMemcpyAsync(b->hlens.data(), dl, sizeof(tl::DevLens) * nlens,
+  E.check(tl::copy_async(b->hlens.data(), dl, sizeof(tl::DevLens) * nlens,
                           cudaMemcpyDeviceToHost, E.stream));
   if (!E.check(cudaStreamSynchronize(E.stream))) return -2;
   return nlens;
@@ -120,12 +120,12 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
     void* dsc = b->scan.need(sizeof(tl::SeedJob) * scan.size());
     void* dpr = b->prep.need(sizeof(tl::PointPrep) * base);
     if (!dsc || !dpr) return -2;
-    E.check(cudaMemcpyAsync(dsc, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+    E.check(tl::copy_async(dsc, scan.data(), sizeof(tl::SeedJob) * scan.size(),
                             cudaMemcpyHostToDevice, E.stream));
   }
-  E.check(cudaMemcpyAsync(dt, b->htraj.data(), sizeof(tl::Traj) * ntraj, cudaMemcpyHostToDevice,
+  E.check(tl::copy_async(dt, b->htraj.data(), sizeof(tl::Traj) * ntraj, cudaMemcpyHostToDevice,
                           E.stream));
-  E.check(cudaMemcpyAsync(dj, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+  E.check(tl::copy_async(dj, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   // the exact chain in kSegments segments: jobs, point lists and counts
   b->nseg = 0;
@@ -146,11 +146,11 @@ long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_
     void* dsn = b->segn.need(sizeof(unsigned) * S);
     void* dch = b->chains.need(sizeof(tl::RootChain) * ntraj);
     if (!dsj || !dsl || !dsn || !dch) return -2;
-    E.check(cudaMemcpyAsync(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(),
+    E.check(tl::copy_async(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(),
                             cudaMemcpyHostToDevice, E.stream));
-    E.check(cudaMemcpyAsync(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
+    E.check(tl::copy_async(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
                             E.stream));
-    E.check(cudaMemcpyAsync(dsn, sn.data(), sizeof(unsigned) * S, cudaMemcpyHostToDevice,
+    E.check(tl::copy_async(dsn, sn.data(), sizeof(unsigned) * S, cudaMemcpyHostToDevice,
                             E.stream));
     b->nseg = S;
   }
@@ -228,7 +228,7 @@ int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, v
   // wait before the pageable copy: a copy that waits for kernels holds the
   // driver's staging path and stalls other threads' copies
   if (!E.check(cudaStreamSynchronize(st))) return -2;
-  if (!E.check(cudaMemcpyAsync(h.data(), b->out.p, sizeof(tl::PointOut) * b->npoints,
+  if (!E.check(tl::copy_async(h.data(), b->out.p, sizeof(tl::PointOut) * b->npoints,
                                cudaMemcpyDeviceToHost, st)))
     return -2;
   if (!E.check(cudaStreamSynchronize(st))) return -2;
@@ -396,7 +396,7 @@ long tlb_point_lc(tl_batch* b, double* amp) {
   double* da = (double*)b->amp.need(sizeof(double) * b->npoints);
   if (!djp || !da) return -2;
   E.check(cudaMemsetAsync(da, 0, sizeof(double) * b->npoints, E.stream));
-  E.check(cudaMemcpyAsync(djp, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+  E.check(tl::copy_async(djp, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
   if (b->chain <= 0)
     tl::launch_point_lc_exact((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp,
@@ -406,7 +406,7 @@ long tlb_point_lc(tl_batch* b, double* amp) {
     tl::launch_point_lc((const tl::Traj*)b->trajs.p, (const tl::SeedJob*)djp, (int)jobs.size(),
                         (const tl::DevLens*)b->lenses.p, da, nullptr, E.stream);
   E.check(cudaStreamSynchronize(E.stream));
-  E.check(cudaMemcpyAsync(amp, da, sizeof(double) * b->npoints, cudaMemcpyDeviceToHost, E.stream));
+  E.check(tl::copy_async(amp, da, sizeof(double) * b->npoints, cudaMemcpyDeviceToHost, E.stream));
   bool ok = E.check(cudaStreamSynchronize(E.stream));
   cudaFree(djp);
   return ok ? b->npoints : -2;

@@ -15,6 +15,8 @@
 
 namespace tl {
 
+std::atomic<unsigned long long> g_copy_h2d{0}, g_copy_d2h{0};
+
 void* DevBuf::need(size_t bytes, cudaStream_t st) {
   if (bytes == 0) bytes = 16;
   if (bytes > n) {

@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -15,6 +16,18 @@
 struct LightCurveIRS;
 
 namespace tl {
+
+// Bytes moved host -> device and device -> host by the C ABIs' own copies
+// (lcirs_*, tlb_*), process-wide totals for end-to-end accounting.
+extern std::atomic<unsigned long long> g_copy_h2d, g_copy_d2h;
+
+// cudaMemcpyAsync with the same arguments, counted.
+inline cudaError_t copy_async(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,
+                              cudaStream_t st = 0) {
+  if (kind == cudaMemcpyHostToDevice) g_copy_h2d.fetch_add(bytes, std::memory_order_relaxed);
+  if (kind == cudaMemcpyDeviceToHost) g_copy_d2h.fetch_add(bytes, std::memory_order_relaxed);
+  return cudaMemcpyAsync(dst, src, bytes, kind, st);
+}
 
 // Grow-only device buffer.  With a stream, the buffer comes from the
 // device's stream-ordered pool (cudaMallocAsync / cudaFreeAsync on that

@@ -79,18 +79,18 @@ void setup_object(LightCurveIRS* o) {
     I->ck(cudaMallocAsync(&I->d_chain, sizeof(tl::RootChain), I->st));
   }
   tl::LensSpec* d_spec = (tl::LensSpec*)I->specbuf.need(sizeof(tl::LensSpec), I->st);
-  I->ck(cudaMemcpyAsync(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, I->st));
+  I->ck(tl::copy_async(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, I->st));
   tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, I->st);
   // every copy into pageable host memory waits for its stream first: such a
   // copy holds the driver's staging path while it waits, and would stall the
   // copies of every other host thread behind a long kernel
   I->ck(cudaStreamSynchronize(I->st));
-  I->ck(cudaMemcpyAsync(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost, I->st));
+  I->ck(tl::copy_async(&I->lens, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToHost, I->st));
   I->ck(cudaStreamSynchronize(I->st));
   // a fresh object's solver: no roots yet, the constructor's heap state
   tl::RootChain ch;
   tl::chain_reset(&ch, I->lens.heap0);
-  I->ck(cudaMemcpyAsync(I->d_chain, &ch, sizeof(ch), cudaMemcpyHostToDevice, I->st));
+  I->ck(tl::copy_async(I->d_chain, &ch, sizeof(ch), cudaMemcpyHostToDevice, I->st));
   I->ck(cudaStreamSynchronize(I->st));
   E.trace("setup_object: done");
   const tl::Grid& g2 = I->lens.g;
@@ -164,7 +164,7 @@ void LightCurveIRS::setLimbDarkening(const std::string& model, double v) {
   impl->spec.ld_a = ldA;
   impl->spec.ld_b = ldB;
   impl->spec.intensity = intensityCoeff;
-  impl->ck(cudaMemcpyAsync(impl->d_lens, &impl->lens, sizeof(tl::DevLens), cudaMemcpyHostToDevice,
+  impl->ck(tl::copy_async(impl->d_lens, &impl->lens, sizeof(tl::DevLens), cudaMemcpyHostToDevice,
                            impl->st));
   impl->ck(cudaStreamSynchronize(impl->st));
 }
@@ -329,19 +329,19 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
   // gather the objects' lenses, caustics and warm-start chains
   for (int i = 0; i < k; i++) {
     const LightCurveIRS::Impl* I = reqs[i]->obj->impl;
-    ck(cudaMemcpyAsync(dl + i, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToDevice, B.st));
-    ck(cudaMemcpyAsync(dca + (size_t)i * tl::kBranches * tl::kCCLen, I->d_ca,
+    ck(tl::copy_async(dl + i, I->d_lens, sizeof(tl::DevLens), cudaMemcpyDeviceToDevice, B.st));
+    ck(tl::copy_async(dca + (size_t)i * tl::kBranches * tl::kCCLen, I->d_ca,
                        sizeof(cx) * tl::kBranches * tl::kCCLen, cudaMemcpyDeviceToDevice, B.st));
-    ck(cudaMemcpyAsync(dch + i, I->d_chain, sizeof(tl::RootChain), cudaMemcpyDeviceToDevice,
+    ck(tl::copy_async(dch + i, I->d_chain, sizeof(tl::RootChain), cudaMemcpyDeviceToDevice,
                        B.st));
   }
-  ck(cudaMemcpyAsync(R.trajs, trajs.data(), sizeof(tl::Traj) * k, cudaMemcpyHostToDevice, B.st));
-  ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+  ck(tl::copy_async(R.trajs, trajs.data(), sizeof(tl::Traj) * k, cudaMemcpyHostToDevice, B.st));
+  ck(tl::copy_async(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                      cudaMemcpyHostToDevice, B.st));
   if (chain <= 0) {
     // the exact chain in segments, each segment's fill beside the next
     // segment's chain; every curve continues from its object's chain state
-    ck(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+    ck(tl::copy_async(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
                        cudaMemcpyHostToDevice, B.st));
     const int S = kBatchSegments;
     std::vector<tl::SeedJob> sj;
@@ -358,11 +358,11 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
     auto* dsj = (tl::SeedJob*)B.segjobs.need(sizeof(tl::SeedJob) * sj.size(), B.st);
     auto* dsl = (int32_t*)B.seglist.need(sizeof(int32_t) * sl.size(), B.st);
     auto* dsn = (unsigned*)B.segn.need(sizeof(unsigned) * S, B.st);
-    ck(cudaMemcpyAsync(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(), cudaMemcpyHostToDevice,
+    ck(tl::copy_async(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(), cudaMemcpyHostToDevice,
                        B.st));
-    ck(cudaMemcpyAsync(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
+    ck(tl::copy_async(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
                        B.st));
-    ck(cudaMemcpyAsync(dsn, sn.data(), sizeof(unsigned) * S, cudaMemcpyHostToDevice, B.st));
+    ck(tl::copy_async(dsn, sn.data(), sizeof(unsigned) * S, cudaMemcpyHostToDevice, B.st));
     tl::Pipeline P;
     P.lenses = dl;
     P.ca = dca;
@@ -388,14 +388,14 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
   }
   // the chains go back to their objects
   for (int i = 0; i < k; i++)
-    ck(cudaMemcpyAsync(reqs[i]->obj->impl->d_chain, dch + i, sizeof(tl::RootChain),
+    ck(tl::copy_async(reqs[i]->obj->impl->d_chain, dch + i, sizeof(tl::RootChain),
                        cudaMemcpyDeviceToDevice, B.st));
   B.hout.resize(total);
   B.hseeds.resize(total * 2 * tl::kMaxSeeds);
   ck(cudaStreamSynchronize(B.st));   // before the pageable copies (see setup_object)
-  ck(cudaMemcpyAsync(B.hout.data(), R.out, sizeof(tl::PointOut) * total, cudaMemcpyDeviceToHost,
+  ck(tl::copy_async(B.hout.data(), R.out, sizeof(tl::PointOut) * total, cudaMemcpyDeviceToHost,
                      B.st));
-  ck(cudaMemcpyAsync(B.hseeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * total,
+  ck(tl::copy_async(B.hseeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * total,
                      cudaMemcpyDeviceToHost, B.st));
   ck(cudaStreamSynchronize(B.st));
   for (int i = 0; i < k; i++) {
@@ -481,11 +481,11 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   if (chainPoints <= 0) tl::plan_jobs(&scan, 0, (long)np, tl::kChainChunk, -1);
   E.trace("runFill: prepare");
   tl::Run R = I->bufs.prepare(np, 1, jobs.size(), amoebaPrintOut_, scan.size(), I->st);
-  I->ck(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
-  I->ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+  I->ck(tl::copy_async(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
+  I->ck(tl::copy_async(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, I->st));
   if (chainPoints <= 0) {
-    I->ck(cudaMemcpyAsync(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
+    I->ck(tl::copy_async(R.scan_jobs, scan.data(), sizeof(tl::SeedJob) * scan.size(),
                             cudaMemcpyHostToDevice, I->st));
     tl::launch_seeds_exact(R.scan_jobs, (int)scan.size(), R.jobs, (int)jobs.size(), R.trajs,
                            impl->d_lens, impl->d_ca, R.points, R.seeds, R.out, R.trials, R.prep,
@@ -498,16 +498,16 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
     // replace the seeds with the caller's, keep the positions
     std::vector<tl::PointOut> hout(np);
     I->ck(cudaStreamSynchronize(I->st));
-    I->ck(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
+    I->ck(tl::copy_async(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
                             I->st));
     I->ck(cudaStreamSynchronize(I->st));
     for (size_t i = 0; i < np; i++) {
       hout[i].nseeds = (uint32_t)std::max(0, std::min(extN[i], tl::kMaxSeeds));
       hout[i].status = 0;
     }
-    I->ck(cudaMemcpyAsync(R.out, hout.data(), sizeof(tl::PointOut) * np, cudaMemcpyHostToDevice,
+    I->ck(tl::copy_async(R.out, hout.data(), sizeof(tl::PointOut) * np, cudaMemcpyHostToDevice,
                             I->st));
-    I->ck(cudaMemcpyAsync(R.seeds, extSeeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
+    I->ck(tl::copy_async(R.seeds, extSeeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
                             cudaMemcpyHostToDevice, I->st));
   }
   E.trace("runFill: seeds launched");
@@ -527,16 +527,16 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   }
   I->ck(cudaStreamSynchronize(I->st));   // before the pageable copies (see setup_object)
   std::vector<tl::PointOut> hout(np);
-  I->ck(cudaMemcpyAsync(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
+  I->ck(tl::copy_async(hout.data(), R.out, sizeof(tl::PointOut) * np, cudaMemcpyDeviceToHost,
                           I->st));
   seeds.resize(np * 2 * tl::kMaxSeeds);
   nseeds.resize(np);
-  I->ck(cudaMemcpyAsync(seeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
+  I->ck(tl::copy_async(seeds.data(), R.seeds, sizeof(int32_t) * 2 * tl::kMaxSeeds * np,
                           cudaMemcpyDeviceToHost, I->st));
   std::vector<uint32_t> dump;
   unsigned ndump = 0;
   if (amoebaPrintOut_) {
-    I->ck(cudaMemcpyAsync(&ndump, R.dump_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
+    I->ck(tl::copy_async(&ndump, R.dump_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
                             I->st));
   }
   I->ck(cudaStreamSynchronize(I->st));
@@ -618,8 +618,8 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   std::vector<tl::SeedJob> jobs;
   tl::plan_jobs(&jobs, 0, (long)n, chainPoints, 0);
   tl::Run R = I->bufs.prepare(n, 1, jobs.size(), false, 0, I->st);
-  I->ck(cudaMemcpyAsync(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
-  I->ck(cudaMemcpyAsync(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
+  I->ck(tl::copy_async(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
+  I->ck(tl::copy_async(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, I->st));
   double* d_amp = (double*)I->ampbuf.need(sizeof(double) * n, I->st);
   if (chainPoints <= 0)
@@ -629,7 +629,7 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
     tl::launch_point_lc(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp, impl->d_chain,
                         I->st);
   I->ck(cudaStreamSynchronize(I->st));   // before the pageable copy (see setup_object)
-  I->ck(cudaMemcpyAsync(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
+  I->ck(tl::copy_async(lcVec.data(), d_amp, sizeof(double) * n, cudaMemcpyDeviceToHost,
                           I->st));
   I->ck(cudaStreamSynchronize(I->st));
   for (size_t i = 0; i < n; i++) impl->lcFull[i] = lcVec[i];
@@ -711,6 +711,12 @@ void lcirs_fill_from_seeds(LightCurveIRS* lc, double iniX, double iniY, double f
 
 void lcirs_copy_stats(LightCurveIRS* lc, uint64_t* out3) {
   for (int k = 0; k < 3; k++) out3[k] = lc->stats[k];
+}
+
+void lcirs_copy_transfer_bytes(uint64_t* out2) {
+  if (!out2) return;
+  out2[0] = tl::g_copy_h2d.load();
+  out2[1] = tl::g_copy_d2h.load();
 }
 
 void lcirs_set_precision(LightCurveIRS* lc, int mode) { lc->precision = mode; }

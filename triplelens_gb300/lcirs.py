@@ -52,8 +52,19 @@ def load_lcirs(path=None):
     L.lcirs_set_precision.argtypes = [vp, ctypes.c_int]
     L.lcirs_set_chain.argtypes = [vp, ctypes.c_int]
     L.lcirs_copy_diag.argtypes = [vp, ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")]
+    L.lcirs_copy_transfer_bytes.argtypes = [ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
+    L.lcirs_copy_transfer_bytes.restype = None
     _libs[path] = L
     return L
+
+
+def transfer_bytes(lib_path=None):
+    """(host -> device, device -> host) bytes the library's own copies have
+    moved in this process so far (lcirs_copy_transfer_bytes): what an
+    end-to-end run sends across the host boundary, counted by the library."""
+    out = np.zeros(2, np.uint64)
+    load_lcirs(lib_path).lcirs_copy_transfer_bytes(out)
+    return int(out[0]), int(out[1])
 
 
 MAX_SEEDS = 64
