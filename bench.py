@@ -64,29 +64,51 @@ def _cpu_worker(args):
     return time.perf_counter() - t0 + t_seeds, len(idx), rays, t_seeds
 
 
+def sample_indices(k, per_curve, n):
+    """Point indices of curve k in the CPU sample: `per_curve` points evenly
+    spaced along the curve, shifted by a golden-ratio offset per curve, so
+    that with one point per curve the sample still covers every position
+    along the trajectories (near and far from the lenses) instead of the
+    curves' first points alone."""
+    step = (n + 1) / float(per_curve)
+    off = ((k + 0.5) * 0.6180339887498949) % 1.0
+    return np.minimum(((np.arange(per_curve) + off) * step).astype(np.int64), n)
+
+
 def cpu_baseline(pool, procs, lenses, trajs, n, sample_points):
     """Times the oracle (image chain + fill) on `sample_points` points spread
-    over the curves, split over `procs` processes; returns (points/s all
-    cores, points/s one core, rays/s all cores, description, busy seconds)."""
+    over the curves, split over `procs` concurrent processes; returns
+    (points/s all cores, points/s one core, rays/s all cores, description,
+    busy seconds).
+
+    A point costs its fill plus its 1/(n+1) share of its curve's warm-start
+    chain (the reference computes every point of a curve in one chain).  A
+    sampled point still needs the chain up to it, so each task runs its
+    curve's whole chain but is charged only the sampled points' shares; the
+    rates divide the sampled points by the charged CPU seconds (each
+    measured inside its process while the others run), times the processes
+    that ran, not by the wall time, which would count the uncharged chain
+    work."""
     ncurves = len(lenses)
     use = min(ncurves, max(1, sample_points))
     per_curve = max(1, sample_points // use)
     tasks = []
     for k in range(use):
-        pts = np.linspace(0, n, per_curve, dtype=np.int64)
+        pts = sample_indices(k, per_curve, n)
         for chunk in np.array_split(pts, max(1, procs // use)):
             if len(chunk):
                 tasks.append((lenses[k], trajs[k], n, chunk.tolist()))
-    t0 = time.perf_counter()
     res = pool.map(_cpu_worker, tasks)
-    wall = time.perf_counter() - t0
     busy = sum(r[0] for r in res)
     npts = sum(r[1] for r in res)
     rays = sum(r[2] for r in res)
     t_seed = sum(r[3] for r in res)
-    desc = ("%d points spread over %d curves: oracle image chain (charged pro rata, %.2f s) + "
-            "oracle fill, %d processes" % (npts, use, t_seed, procs))
-    return npts / wall, npts / busy, rays / wall, desc, busy
+    par = min(procs, len(tasks))
+    desc = ("%d points spread along %d curves (%d per curve): oracle fill + each point's share "
+            "of its curve's image chain (%.3f s of %.2f s charged CPU time), %d concurrent "
+            "processes; points/s = points x processes / charged CPU seconds"
+            % (npts, use, per_curve, t_seed, busy, par))
+    return npts * par / busy, npts / busy, rays * par / busy, desc, busy
 
 
 class quiet_stdout:
@@ -482,7 +504,8 @@ def main():
     ap.add_argument("--chain", type=int, default=0,
                     help="warm-start chain: 0 = one per curve (the reference's, exact), "
                          "k > 0 = restart every k points")
-    ap.add_argument("--cpu-sample", type=int, default=256, help="points timed on the CPU")
+    ap.add_argument("--cpu-sample", type=int, default=608,
+                    help="points timed on the CPU (spread over the curves)")
     ap.add_argument("--e2e-threads", type=int, default=0,
                     help="host threads of the e2e leg (0: one per curve)")
     ap.add_argument("--no-cpu", action="store_true")

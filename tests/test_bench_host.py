@@ -1,9 +1,12 @@
 """bench.py host-side helpers (no GPU): the HBM view of the fill's DRAM
-traffic and the reference arm's JSON line shape."""
+traffic, the CPU legs' point sample and the reference arm's JSON line
+shape."""
 import json
 import os
 import subprocess
 import sys
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
@@ -55,3 +58,18 @@ def test_parity_vs_fixture_counts_mismatches():
     cnt[5] += 1
     assert bench.parity_vs_fixture(cnt, n, 11, 2024, 0)["mismatches"] == 1
     assert bench.parity_vs_fixture(cnt, n, 11, 7, 0) is None
+
+
+def test_cpu_sample_covers_the_whole_curve():
+    """The CPU legs sample points along the whole trajectory: one point per
+    curve over 152 curves lands in every tenth of the curve, several points
+    per curve are distinct and in range, and n+1 points take every point."""
+    import bench
+    n = 5000
+    one = np.array([bench.sample_indices(k, 1, n)[0] for k in range(152)])
+    hist = np.histogram(one, bins=10, range=(0, n + 1))[0]
+    assert hist.min() >= 10 and one.min() >= 0 and one.max() <= n
+    for k in range(20):
+        s = bench.sample_indices(k, 7, n)
+        assert len(set(s.tolist())) == 7 and s.min() >= 0 and s.max() <= n
+    assert sorted(bench.sample_indices(3, n + 1, n).tolist()) == list(range(n + 1))
