@@ -1080,18 +1080,19 @@ static cx cpow2(cx w) {
   return mk(r * cos(t), r * sin(t));
 }
 
+static double image_amp(const orc_lcirs *o, cx img) {
+  cx s = cadd(cadd(rdiv(o->m1, cpow2(csub(img, o->z1))), rdiv(o->m2, cpow2(csub(img, o->z2)))),
+              rdiv(o->m3, cpow2(csub(img, o->z3))));
+  double t = 1.0 / fabs(1.0 - cnorm(s));
+  if (t != t) t = 0.0;
+  return t;
+}
+
 static double point_amp(orc_lcirs *o, cx pos) {
   cx imgs[10];
   int n = get_images(o, pos, imgs);
   double amp = 0.0;
-  for (int k = 0; k < n; k++) {
-    cx img = imgs[k];
-    cx s = cadd(cadd(rdiv(o->m1, cpow2(csub(img, o->z1))), rdiv(o->m2, cpow2(csub(img, o->z2)))),
-                rdiv(o->m3, cpow2(csub(img, o->z3))));
-    double t = 1.0 / fabs(1.0 - cnorm(s));
-    if (t != t) t = 0.0;
-    amp += t;
-  }
+  for (int k = 0; k < n; k++) amp += image_amp(o, imgs[k]);
   return amp;
 }
 
@@ -1140,7 +1141,8 @@ int orc_images_cold(double a, double b, double th, double m2, double m3,
 
 void orc_solve_roots(const double *coeffs, int deg, const double *init,
                      double *roots) {
-  cx c[ORC_MAXC], in[ORC_MAXC], r[ORC_MAXC];
+  cx c[ORC_MAXC] = {{0.0, 0.0}}, in[ORC_MAXC], r[ORC_MAXC];
+  if (deg < 1 || deg >= ORC_MAXC) return;
   for (int k = 0; k <= deg; k++) c[k] = mk(coeffs[2 * k], coeffs[2 * k + 1]);
   if (init)
     for (int k = 0; k <= deg; k++) in[k] = mk(init[2 * k], init[2 * k + 1]);
@@ -1150,6 +1152,7 @@ void orc_solve_roots(const double *coeffs, int deg, const double *init,
 
 int orc_laguerre(const double *coeffs, int deg, double *x) {
   cx c[ORC_MAXC];
+  if (deg < 1 || deg >= ORC_MAXC) return 0;
   for (int k = 0; k <= deg; k++) c[k] = mk(coeffs[2 * k], coeffs[2 * k + 1]);
   cx z = mk(x[0], x[1]);
   int ok = lag_iter(c, deg, &z);
@@ -1162,4 +1165,26 @@ void orc_lens_poly(const orc_lcirs *o, double sx, double sy, double *c) {
   cx cc[11];
   lens_poly(o, mk(sx, sy), cc);
   for (int k = 0; k < 11; k++) { c[2 * k] = cc[k].re; c[2 * k + 1] = cc[k].im; }
+}
+
+/* Test hooks: the helpers above, for the host comparison tests. */
+int orc_intersection_check(const orc_lcirs *o, double sx, double sy, double ax, double ay,
+                           double bx, double by, double *trial_xy) {
+  cx t = mk(0.0, 0.0);
+  int hit = intersection_check(o, mk(sx, sy), mk(ax, ay), mk(bx, by), &t);
+  trial_xy[0] = t.re;
+  trial_xy[1] = t.im;
+  return hit;
+}
+
+double orc_image_amp(const orc_lcirs *o, double ix, double iy) {
+  return image_amp(o, mk(ix, iy));
+}
+
+void orc_grid_maps(const orc_lcirs *o, int64_t nx, int64_t ny, double x, double y,
+                   double *xy_out, int64_t *n_out) {
+  xy_out[0] = nx_to_x(o, nx);
+  xy_out[1] = ny_to_y(o, ny);
+  n_out[0] = x_to_nx(o, x);
+  n_out[1] = y_to_ny(o, y);
 }

@@ -104,6 +104,18 @@ int orc_laguerre(const double *coeffs, int deg, double *x);
 /* Degree-10 lens polynomial coefficients for source zeta. */
 void orc_lens_poly(const orc_lcirs *o, double sx, double sy, double *c /*22*/);
 
+/* lcirs.cc:195-255 (Q5 geometry) for the segment A-B and the object's rho;
+ * returns 1 on a hit and writes the trial point. */
+int orc_intersection_check(const orc_lcirs *o, double sx, double sy, double ax, double ay,
+                           double bx, double by, double *trial_xy);
+
+/* lcbase.cc:17-38: one image's term of the point-source magnification. */
+double orc_image_amp(const orc_lcirs *o, double ix, double iy);
+
+/* lcirs.cc:355-379: grid maps of the object's image plane. */
+void orc_grid_maps(const orc_lcirs *o, int64_t nx, int64_t ny, double x, double y,
+                   double *xy_out, int64_t *n_out);
+
 #ifdef __cplusplus
 }
 #endif
