@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <mutex>
+#include <stdexcept>
 #include <vector>
 
 #include "batch_internal.h"
@@ -19,6 +21,18 @@ namespace {
 
 cudaStream_t pick(void* s) {
   return s ? (cudaStream_t)s : tl::Engine::get().stream;
+}
+
+// Runs an entry point's body; an exception (host memory exhausted) does not
+// cross the C ABI but returns `fail`, as a CUDA failure does.
+template <class R, class F>
+R guarded(R fail, F body) {
+  try {
+    return body();
+  } catch (const std::exception& ex) {
+    fprintf(stderr, "tl_batch: %s\n", ex.what());
+    return fail;
+  }
 }
 
 }  // namespace
@@ -39,7 +53,7 @@ void tlb_delete(tl_batch* b) {
   delete b;
 }
 
-int tlb_set_lenses(tl_batch* b, int nlens, const double* p8) {
+static int set_lenses_body(tl_batch* b, int nlens, const double* p8) {
   if (!b || nlens <= 0 || !p8) return -1;
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
@@ -81,8 +95,8 @@ int tlb_set_lenses(tl_batch* b, int nlens, const double* p8) {
 // segments of an exact chain for tlb_run_device phase 4
 constexpr int kSegments = 8;
 
-long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
-                          const uint32_t* n) {
+static long set_trajectories_body(tl_batch* b, int ntraj, const double* t4,
+                                  const int32_t* lens_idx, const uint32_t* n) {
   if (!b || ntraj <= 0 || !t4 || !lens_idx || !n || b->nlens <= 0) return -1;
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
@@ -220,7 +234,8 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
   return E.check(cudaGetLastError()) ? 0 : -2;
 }
 
-int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, void* stream) {
+static int download_body(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status,
+                         void* stream) {
   if (!b || b->npoints <= 0) return -1;
   tl::Engine& E = tl::Engine::get();
   cudaStream_t st = pick(stream);
@@ -250,9 +265,9 @@ int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, v
   return 0;
 }
 
-long tlb_run_host(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
-                  const uint32_t* n, double* amp, uint64_t* counts, uint32_t* status,
-                  void* stream) {
+static long run_host_body(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
+                          const uint32_t* n, double* amp, uint64_t* counts, uint32_t* status,
+                          void* stream) {
   long np = tlb_set_trajectories(b, ntraj, t4, lens_idx, n);
   if (np < 0) return np;
   int r = tlb_run_device(b, 3, stream);
@@ -383,7 +398,7 @@ int tlb_graph_launch(tl_batch* b, void* stream) {
   return ok ? 0 : -2;
 }
 
-long tlb_point_lc(tl_batch* b, double* amp) {
+static long point_lc_body(tl_batch* b, double* amp) {
   if (!b || b->ntraj <= 0 || !amp) return -1;
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
@@ -410,6 +425,32 @@ long tlb_point_lc(tl_batch* b, double* amp) {
   bool ok = E.check(cudaStreamSynchronize(E.stream));
   cudaFree(djp);
   return ok ? b->npoints : -2;
+}
+
+// entry points that allocate host memory
+int tlb_set_lenses(tl_batch* b, int nlens, const double* p8) {
+  return guarded(-2, [&] { return set_lenses_body(b, nlens, p8); });
+}
+
+long tlb_set_trajectories(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
+                          const uint32_t* n) {
+  return guarded(-2L, [&] { return set_trajectories_body(b, ntraj, t4, lens_idx, n); });
+}
+
+int tlb_download(tl_batch* b, double* amp, uint64_t* counts, uint32_t* status, void* stream) {
+  return guarded(-2, [&] { return download_body(b, amp, counts, status, stream); });
+}
+
+long tlb_run_host(tl_batch* b, int ntraj, const double* t4, const int32_t* lens_idx,
+                  const uint32_t* n, double* amp, uint64_t* counts, uint32_t* status,
+                  void* stream) {
+  return guarded(-2L, [&] {
+    return run_host_body(b, ntraj, t4, lens_idx, n, amp, counts, status, stream);
+  });
+}
+
+long tlb_point_lc(tl_batch* b, double* amp) {
+  return guarded(-2L, [&] { return point_lc_body(b, amp); });
 }
 
 }  // extern "C"

@@ -19,6 +19,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <mutex>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -449,7 +450,14 @@ void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
                  B.pending.size());
         E.trace(msg);
       }
-      run_batch(B, mine);
+      try {
+        run_batch(B, mine);
+      } catch (const std::exception& ex) {
+        // host allocation failure: the callers get the error bit, and the
+        // batcher stays usable (no caller is left waiting on this batch)
+        fprintf(stderr, "liblcirs: batch of %zu curves failed: %s\n", mine.size(), ex.what());
+        for (Request* q : mine) q->obj->lastStatus = 0x100u;
+      }
       E.trace("batch done");
       lk.lock();
       for (Request* q : mine) q->done = true;
