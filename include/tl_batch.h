@@ -17,7 +17,8 @@
  * n = 0 is one source position (x0, y0) (one point, its own chain).
  *
  * Return values: >= 0 success (number of points for runs), < 0 error
- * (-1 bad argument, -2 CUDA error).
+ * (-1 bad argument, -2 CUDA error or host memory exhausted; no C++
+ * exception leaves these functions).
  */
 #ifndef TL_BATCH_H
 #define TL_BATCH_H
