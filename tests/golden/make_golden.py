@@ -14,6 +14,7 @@ Three reference builds (oracle/Makefile.ref): "strict" (IEEE, -O2
 show the reference's own build-to-build spread.
 
     python tests/golden/make_golden.py --ref <TripleLens checkout> [--c2] [--bench]
+        [--only-ccc | --only-bench | --only-extra]
 
 (--ref may be replaced by TRIPLELENS_REF in the environment.)  Each reference
 run happens in a child process of its own (its stdout is C++ cout, and its
@@ -228,6 +229,34 @@ def ccc_and_images(lib, lens, positions):
     return cc, ca, roots, isimg
 
 
+# small cases that no other fixture covers: a binary lens (m3 == 0: the
+# two-lens ray map, lcirs.cc:28-36, and the binary image count), a two-point
+# curve (n = 1) and a curve far from the caustics.  The far curve has n = 6:
+# at n = 5 the reference's own write past lcVec (lcirs.cc:117,181, quirk Q1)
+# lands on the next heap chunk's header, because 5 doubles fill their malloc
+# chunk exactly, and glibc aborts the process ("corrupted size vs. prev_size");
+# for most n the write falls into the chunk's rounding slack
+EXTRA_CASES = [
+    ("binary", [1.2, 0.9, 1.0, 0.3, 0.0, 0.01, 0.0, 60.0], [-1.5, 0.05, 1.5, 0.15], 40),
+    ("short", [1.0, 1.0, 1.2, 0.1, 0.05, 0.02, 0.3, 40.0], [0.1, 0.2, 0.3, 0.1], 1),
+    ("far", [1.0, 1.0, 1.2, 0.1, 0.05, 0.02, 0.3, 40.0], [1.8, 1.9, 2.1, 1.7], 6),
+]
+
+
+def extra_fixtures():
+    out = {}
+    jobs = {}
+    for name, lens, traj, n in EXTRA_CASES:
+        out["lens_" + name] = np.array(lens)
+        out["traj_" + name] = np.array(traj)
+        out["n_" + name] = np.array(n)
+        for build, lib in REF_LIBS.items():
+            jobs[(name, build)] = POOL.submit(run_curve, lib, np.array(lens), np.array(traj), n)
+    for (name, build), f in jobs.items():
+        out["counts_%s_%s" % (name, build)], out["amps_%s_%s" % (name, build)] = f.result()
+    return out
+
+
 def curves(lib, lenses, trajs, n):
     """Reference curves, several child processes at a time."""
     futs = [POOL.submit(run_curve, lib, lenses[k], trajs[k], n) for k in range(len(lenses))]
@@ -246,6 +275,8 @@ def main():
     ap.add_argument("--only-ccc", action="store_true")
     ap.add_argument("--only-bench", action="store_true",
                     help="only the benchmark fixture (implies --bench)")
+    ap.add_argument("--only-extra", action="store_true",
+                    help="only extra_cases.npz (binary lens, short and far curves)")
     args = ap.parse_args()
     if args.worker:
         worker(json.loads(args.worker))
@@ -264,6 +295,10 @@ def main():
     if args.only_bench:
         args.bench = True
         bench_fixture()
+        return
+    np.savez_compressed(os.path.join(HERE, "extra_cases.npz"), **extra_fixtures())
+    print("wrote extra_cases.npz")
+    if args.only_extra:
         return
     np.savez_compressed(os.path.join(HERE, "ccc.npz"), **ccc_fixtures(REF_LIBS["fast"]))
     print("wrote ccc.npz")

@@ -274,17 +274,24 @@ def test_binary_lens_m3_zero(product_lib, oracle_lib):
     o = _oracle(oracle_lib, lens, n)
     _, ocounts = o.lc_irs(*traj)
     assert np.array_equal(lc.counts(), ocounts)
+    # and the reference's own counts (strict build, tests/golden/extra_cases.npz)
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "extra_cases.npz"))
+    assert np.array_equal(z["lens_binary"], lens) and int(z["n_binary"]) == n
+    assert np.array_equal(lc.counts(), z["counts_binary_strict"])
 
 
 def test_short_and_far_curves(product_lib, oracle_lib):
     # n = 1 (two points) and a source far from the caustics (A close to 1)
     lens = np.array([1.0, 1.0, 1.2, 0.1, 0.05, 0.02, 0.3, 40.0])
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "extra_cases.npz"))
     for traj, n in ((np.array([0.1, 0.2, 0.3, 0.1]), 1), (np.array([1.8, 1.9, 2.1, 1.7]), 5)):
         lc = _lc(product_lib, lens, n, 1)
         lc.get_lc_irs(*traj)
         o = _oracle(oracle_lib, lens, n)
         _, ocounts = o.lc_irs(*traj)
         assert np.array_equal(lc.counts(), ocounts)
+        if n == 1:   # the reference's own counts (strict build)
+            assert np.array_equal(lc.counts(), z["counts_short_strict"])
 
 
 def test_bad_input_reports_status(product_lib):

@@ -126,6 +126,20 @@ def test_config2_short_matches_reference(oracle_lib):
         assert np.array_equal(amps[:n], z["amps_%d" % k]), k
 
 
+@pytest.mark.parametrize("case", ["binary", "short", "far"])
+def test_extra_cases_match_reference(oracle_lib, case):
+    """A binary lens (m3 = 0: the two-lens ray map and image count), a
+    two-point curve and a curve far from the caustics: counts and
+    magnifications equal the strict reference build's on every point."""
+    z = np.load(os.path.join(GOLDEN, "extra_cases.npz"))
+    L, t, n = z["lens_" + case], z["traj_" + case], int(z["n_" + case])
+    o = oracle_lib.OracleIRS(*L[:5], L[5], n, int(L[7]))
+    o.set_limb_darkening("linear", L[6])
+    amps, counts = o.lc_irs(*t)
+    assert np.array_equal(counts, z["counts_%s_strict" % case])
+    assert np.array_equal(amps[:n], z["amps_%s_strict" % case])
+
+
 def _sampled_counts(oracle_lib, L, t, n, points):
     """Counts at the given points: the whole warm-start chain (every point's
     seeds, in order), then the fill of the sampled points only."""
