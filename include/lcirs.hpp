@@ -5,12 +5,50 @@
 // and the light curve in lcVec.  The work runs on the GPU engine.
 #pragma once
 
+#include <cmath>
 #include <complex>
 #include <cstdint>
 #include <string>
 #include <vector>
 
 #include "lcirs.h"
+
+// Limb-darkening model, the reference's LimbDarkeningModel
+// (src/LimbDarkening/limbdarkeningmodel.h, .cc:8-49): a source pixel at
+// radius r (in source radii) has brightness A + B sqrt(1 - r^2); intensityCoeff
+// scales the ray sum so that a source of any profile has the flux of a
+// uniform one.
+struct LimbDarkeningModel {
+  enum limbDarkeningModel { linear, linearNormalized, kurucz };
+  limbDarkeningModel model;
+  double intensityCoeff;
+
+  // A = 0.6, B = 0.4
+  LimbDarkeningModel() : model(linear), A_(0.6), B_(0.4) {
+    intensityCoeff = 1.0 / (A_ + 2.0 / 3.0 * B_);
+  }
+  // normalised linear model: I0 (1 - v (1 - sqrt(1 - r^2))), I0 = 1/(1 - v/3)
+  explicit LimbDarkeningModel(double v) : model(linearNormalized), intensityCoeff(1.0) {
+    const double i0 = 1.0 / ((1.0 - v / 3.0));
+    A_ = i0 * (1.0 - v);
+    B_ = i0 * v;
+  }
+  // linear model with central intensity i0
+  LimbDarkeningModel(double i0, double v) : model(linear), A_(i0 * (1.0 - v)), B_(i0 * v) {
+    intensityCoeff = 1.0 / (i0 * (1.0 - v / 3.0));
+  }
+  double sourceBrightness(double r) const;
+  double sourceBrightnessRSq(double rsq) const { return A_ + B_ * std::sqrt(1.0 - rsq); }
+  double getParA() const { return A_; }
+  double getParB() const { return B_; }
+
+ private:
+  double A_, B_;
+};
+
+inline double LimbDarkeningModel::sourceBrightness(double r) const {
+  return A_ + B_ * std::sqrt(1.0 - r * r);
+}
 
 struct LightCurveIRS {
   LightCurveIRS(double a, double b, double th, double m2, double m3, double sourceSize,
@@ -23,6 +61,8 @@ struct LightCurveIRS {
   void getLC(std::complex<double> startPos, std::complex<double> endPos);
   // "linear" -> v-normalised linear model; anything else -> A=0.6, B=0.4
   void setLimbDarkening(const std::string& model, double v);
+  // the reference's setter (lcirs.cc:94-101): any of the model's forms
+  void setLimbDarkeningModel(LimbDarkeningModel ldm);
   void setAmoebaPrintOut(bool amoebaPrintOut, std::string amoebaFilename,
                          std::string parFilename);
 
@@ -60,6 +100,9 @@ struct LightCurveIRS {
   void runBatched(std::complex<double> s, std::complex<double> e);
 
  private:
+  // A, B and the intensity coefficient into the object and its device lens;
+  // the amplitude scale follows (lcirs.cc:94-101)
+  void applyLimbDarkening(double A, double B, double intensity);
   void printOutLCParameters();
   bool amoebaPrintOut_ = false;
   std::string amoebaFilename_, parFilename_;

@@ -126,3 +126,64 @@ def test_transfer_byte_counters_read_without_a_gpu(product_lib):
     import torch
     if not torch.cuda.is_available():
         assert (h2d, d2h) == (0, 0)
+
+
+CXX_CALLER = r"""
+// a C++ caller of the reference's class (src/main.cc:165-176 pattern)
+#include <cstdio>
+#include <cmath>
+#include "lcirs.hpp"
+
+// never called here (no GPU): compiled and linked against liblcirs.so
+void run_curve(double a, double b, double th, double m2, double m3, std::vector<double>* out) {
+  LightCurveIRS lcIRS(a, b, th, m2, m3, 0.001, 100, 50);
+  lcIRS.setLimbDarkeningModel(LimbDarkeningModel(0.5));
+  lcIRS.setAmoebaPrintOut(false, "amoeba", "pars.json");
+  lcIRS.getLCIRS({-1.0, -1.0}, {1.0, 1.0});
+  *out = lcIRS.lcVec;
+  lcIRS.getLC({-1.0, -1.0}, {1.0, 1.0});
+}
+
+static bool same(double x, double y) { return x == y; }
+
+int main(int argc, char**) {
+  if (argc > 5) { std::vector<double> v; run_curve(1, 1, 1, 0.1, 0.1, &v); }
+  // limbdarkeningmodel.cc:8-37
+  LimbDarkeningModel d, n(0.5), l(2.0, 0.4);
+  const double i0 = 1.0 / (1.0 - 0.5 / 3.0);
+  bool ok = same(d.getParA(), 0.6) && same(d.getParB(), 0.4) &&
+            same(d.intensityCoeff, 1.0 / (0.6 + 2.0 / 3.0 * 0.4)) &&
+            d.model == LimbDarkeningModel::linear &&
+            same(n.getParA(), i0 * 0.5) && same(n.getParB(), i0 * 0.5) &&
+            same(n.intensityCoeff, 1.0) && n.model == LimbDarkeningModel::linearNormalized &&
+            same(l.getParA(), 2.0 * 0.6) && same(l.getParB(), 2.0 * 0.4) &&
+            same(l.intensityCoeff, 1.0 / (2.0 * (1.0 - 0.4 / 3.0))) &&
+            same(n.sourceBrightness(0.6), n.getParA() + n.getParB() * std::sqrt(1.0 - 0.36)) &&
+            same(n.sourceBrightnessRSq(0.25), n.getParA() + n.getParB() * std::sqrt(0.75));
+  printf(ok ? "OK\n" : "FAIL\n");
+  return ok ? 0 : 1;
+}
+"""
+
+
+def test_cpp_callers_compile_and_link_against_the_class(product_lib, tmp_path):
+    """include/lcirs.hpp keeps the reference's C++ interface: a main.cc-style
+    caller (constructor, setLimbDarkeningModel with the reference's
+    LimbDarkeningModel, setAmoebaPrintOut, getLCIRS, getLC, lcVec) compiles
+    and links against liblcirs.so; the model's three forms give the
+    reference's coefficients (run without a GPU: the curve is not computed)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    src = tmp_path / "caller.cc"
+    src.write_text(CXX_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(product_lib)
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", INCLUDE, str(src), "-o", str(exe),
+                        "-L", libdir, "-llcirs", "-Wl,-rpath," + libdir,
+                        "-Wl,--allow-shlib-undefined"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr

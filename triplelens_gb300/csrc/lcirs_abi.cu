@@ -145,17 +145,18 @@ LightCurveIRS::~LightCurveIRS() {
 
 void LightCurveIRS::setLimbDarkening(const std::string& model, double v) {
   tl::Engine::get().trace("setLimbDarkening");
-  if (model == "linear") {
-    // limbdarkeningmodel.cc:18-28
-    const double i0 = 1.0 / ((1.0 - v / 3.0));
-    ldA = i0 * (1.0 - v);
-    ldB = i0 * v;
-    intensityCoeff = 1.0;
-  } else {
-    ldA = 0.6;
-    ldB = 0.4;
-    intensityCoeff = 1.0 / (ldA + 2.0 / 3.0 * ldB);
-  }
+  // limbdarkeningmodel.cc:18-28 ("linear") and 8-15 (anything else)
+  setLimbDarkeningModel(model == "linear" ? LimbDarkeningModel(v) : LimbDarkeningModel());
+}
+
+void LightCurveIRS::setLimbDarkeningModel(LimbDarkeningModel ldm) {
+  applyLimbDarkening(ldm.getParA(), ldm.getParB(), ldm.intensityCoeff);
+}
+
+void LightCurveIRS::applyLimbDarkening(double A, double B, double intensity) {
+  ldA = A;
+  ldB = B;
+  intensityCoeff = intensity;
   // _ampScale = intensityCoeff/pi/ppr^2 (lcirs.cc:94-101)
   const double ppr = (double)(int)pointsPerRadius;
   grid[6] = intensityCoeff / 3.14159265358979323846 / (ppr * ppr);
