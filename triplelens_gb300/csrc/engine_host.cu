@@ -234,6 +234,7 @@ void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
 }
 
 void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
+  NvtxRange range("tl fill");
   const bool warp = warp_fill_ != 0;
   const bool team = warp && team_fill_ != 0;
   if (warp && !ensure_wscratch()) return;
@@ -269,8 +270,11 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
       cudaMemsetAsync(wprof, 0, 8 * sizeof(unsigned long long), st);
       w.prof = wprof;
     }
-    launch_wfill(R.points, (int)np, d_lenses, R.seeds, R.out, w, mode, st, order_list,
-                 order_meta);
+    {
+      NvtxRange stage("tl warp fill");
+      launch_wfill(R.points, (int)np, d_lenses, R.seeds, R.out, w, mode, st, order_list,
+                   order_meta);
+    }
     if (profiling) {
       cudaEventRecord(pe[1], st);
       unsigned long long h[8];
@@ -293,8 +297,11 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
       cudaMemsetAsync(prof, 0, 8 * sizeof(unsigned long long), st);
       s.prof = prof;
     }
-    launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st, order_list,
-                order_meta);
+    {
+      NvtxRange stage("tl cta fill");
+      launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st,
+                  order_list, order_meta);
+    }
     if (profiling) {
       unsigned long long h[8];
       cudaMemcpyAsync(h, prof, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -341,6 +348,7 @@ void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mod
     t.dump = R.dump;
     t.dump_count = R.dump_count;
     t.dump_cap = R.dump_cap;
+    NvtxRange stage("tl team fill");
     launch_collect_overflow(R.out, (int)np, list, count, st);
     launch_tfill(R.points, (int)np, d_lenses, R.seeds, R.out, t, mode, st, list, count);
   }
@@ -353,6 +361,8 @@ void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mod
     sl.dump = R.dump;
     sl.dump_count = R.dump_count;
     sl.dump_cap = R.dump_cap;
+    NvtxRange stage(level == 0 ? "tl cta fill" : level == 1 ? "tl cta fill level 1"
+                                                             : "tl cta fill level 2");
     launch_collect_overflow(R.out, (int)np, list, count, st);
     launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, sl, mode, threads_, st, list, count);
   }
@@ -360,6 +370,7 @@ void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mod
 
 void Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode,
                             cudaStream_t st) {
+  NvtxRange range("tl seeds and fill");
   const bool team = team_fill_ != 0;
   if (!ensure_wscratch()) return;
   if (team && !ensure_tscratch()) return;
@@ -393,6 +404,7 @@ void Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode
     }
   }
   for (int s = 0; s < P.nseg; s++) {
+    NvtxRange segment("tl chain segment and its warp fill");
     launch_chain(P.segjobs + P.segjob0[s], P.segjob0[s + 1] - P.segjob0[s], R.trajs, P.lenses,
                  R.points, R.seeds, R.out, R.trials, P.prep, P.chains, st);
     if (profiling) cudaEventRecord(tc[s], st);

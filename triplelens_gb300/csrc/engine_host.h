@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdio>
@@ -20,6 +21,16 @@ namespace tl {
 // Bytes moved host -> device and device -> host by the C ABIs' own copies
 // (lcirs_*, tlb_*), process-wide totals for end-to-end accounting.
 extern std::atomic<unsigned long long> g_copy_h2d, g_copy_d2h;
+
+// NVTX range over a host scope (header-only NVTX 3; a no-op unless a
+// profiler is attached): the kernels launched inside it carry its name, so
+// `ncu --nvtx --nvtx-include "<name>/"` selects one stage of the pipeline.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // cudaMemcpyAsync with the same arguments, counted.
 inline cudaError_t copy_async(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,

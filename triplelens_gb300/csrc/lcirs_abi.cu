@@ -81,7 +81,10 @@ void setup_object(LightCurveIRS* o) {
   }
   tl::LensSpec* d_spec = (tl::LensSpec*)I->specbuf.need(sizeof(tl::LensSpec), I->st);
   I->ck(tl::copy_async(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, I->st));
-  tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, I->st);
+  {
+    tl::NvtxRange range("tl lens set-up");
+    tl::launch_lens_setup(d_spec, 1, I->d_lens, I->d_cc, I->d_ca, I->st);
+  }
   // every copy into pageable host memory waits for its stream first: such a
   // copy holds the driver's staging path while it waits, and would stall the
   // copies of every other host thread behind a long kernel
@@ -294,6 +297,7 @@ Batcher& batcher() {
 constexpr int kBatchSegments = 8;
 
 void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
+  tl::NvtxRange range("tl object batch");
   tl::Engine& E = tl::Engine::get();
   if (!B.st) cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking);
   const int k = (int)reqs.size();
