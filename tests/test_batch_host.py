@@ -1,0 +1,55 @@
+"""The batched API's Python wrapper (triplelens_gb300/batch.py) checks the
+shapes of what it hands to the C functions, which read and write as many
+rows as the counts they are given: wrong shapes raise ValueError before any
+pointer crosses the boundary.  No GPU: the checks are module functions."""
+import numpy as np
+import pytest
+
+from triplelens_gb300 import batch as B
+
+
+def test_lens_rows():
+    one = [1.0, 0.9, 1.0, 0.3, 0.0, 0.01, 0.0, 60.0]
+    a = B._lens_rows(one)                       # one lens as one row
+    assert a.shape == (1, 8) and a.dtype == np.float64 and a.flags.c_contiguous
+    a = B._lens_rows(np.tile(one, (3, 1)).T.copy().T)   # non-contiguous input
+    assert a.shape == (3, 8) and a.flags.c_contiguous
+    for bad in ([1.0, 2.0], np.zeros((2, 7)), np.zeros((0, 8)), np.zeros((2, 8, 1))):
+        with pytest.raises(ValueError):
+            B._lens_rows(bad)
+
+
+def test_traj_args_broadcast_and_check():
+    t, li, nn = B._traj_args([0.0, 0.1, 1.0, 0.2], 0, 100)
+    assert t.shape == (1, 4) and li.tolist() == [0] and nn.tolist() == [100]
+    trajs = np.zeros((3, 4))
+    t, li, nn = B._traj_args(trajs, [0, 1, 2], 50)
+    assert li.dtype == np.int32 and nn.dtype == np.uint32 and nn.tolist() == [50, 50, 50]
+    assert li.flags.c_contiguous and nn.flags.c_contiguous
+    t, li, nn = B._traj_args(trajs, 0, [1, 2, 3])
+    assert li.tolist() == [0, 0, 0] and nn.tolist() == [1, 2, 3]
+    with pytest.raises(ValueError):
+        B._traj_args(np.zeros((3, 3)), 0, 10)        # not 4 values per row
+    with pytest.raises(ValueError):
+        B._traj_args(trajs, [0, 1], 10)              # 2 lens indices for 3 curves
+    with pytest.raises(ValueError):
+        B._traj_args(trajs, 0, [10, 20])             # 2 counts for 3 curves
+    with pytest.raises(ValueError):
+        B._traj_args(trajs, 0, -1)                   # negative count
+    with pytest.raises(ValueError):
+        B._traj_args(np.zeros((0, 4)), 0, 1)
+
+
+def test_output_arrays_are_checked():
+    B._check_out("amp", None, np.float64, 10)    # skipped output
+    B._check_out("amp", np.zeros(12), np.float64, 10)
+    for bad in (np.zeros(9), np.zeros(10, np.float32), np.zeros((10, 2))[:, 0], [0.0] * 10):
+        with pytest.raises(ValueError):
+            B._check_out("amp", bad, np.float64, 10)
+    ro = np.zeros(10)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        B._check_out("amp", ro, np.float64, 10)
+    B._check_out("cnt", np.zeros(10, np.uint64), np.uint64, 10)
+    with pytest.raises(ValueError):
+        B._check_out("cnt", np.zeros(10, np.int64), np.uint64, 10)

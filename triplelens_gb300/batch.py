@@ -56,6 +56,44 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+# The C functions read and write as many rows as the counts they are given:
+# the shapes are checked here, before any pointer crosses the boundary.
+def _lens_rows(lenses):
+    """Lenses as a contiguous (k, 8) float64 array (one row is one lens)."""
+    a = np.ascontiguousarray(np.atleast_2d(np.asarray(lenses, np.float64)))
+    if a.ndim != 2 or a.shape[1] != 8 or a.shape[0] == 0:
+        raise ValueError("lenses: rows of 8 values (a, b, th, m2, m3, rho, ld_v, ppr), "
+                         "got shape %s" % (a.shape,))
+    return a
+
+
+def _traj_args(trajs, lens_idx, n):
+    """Trajectories as a contiguous (k, 4) float64 array, with the lens index
+    and the point count of each curve (a scalar applies to every curve)."""
+    t = np.ascontiguousarray(np.atleast_2d(np.asarray(trajs, np.float64)))
+    if t.ndim != 2 or t.shape[1] != 4 or t.shape[0] == 0:
+        raise ValueError("trajs: rows of 4 values (x0, y0, x1, y1), got shape %s" % (t.shape,))
+    k = t.shape[0]
+    try:
+        li = np.broadcast_to(np.asarray(lens_idx), (k,))
+        nn = np.broadcast_to(np.asarray(n), (k,))
+    except ValueError:
+        raise ValueError("lens_idx and n: one value per curve (%d) or one for all" % k)
+    if np.any(nn < 0) or np.any(nn >= 2 ** 31):
+        raise ValueError("n: point counts in [0, 2^31)")
+    return t, np.ascontiguousarray(li, np.int32), np.ascontiguousarray(nn, np.uint32)
+
+
+def _check_out(name, arr, dtype, points):
+    """An output array the C side writes `points` entries of (None: skipped)."""
+    if arr is None:
+        return
+    if not isinstance(arr, np.ndarray) or arr.dtype != dtype or not arr.flags.c_contiguous \
+            or not arr.flags.writeable or arr.size < points:
+        raise ValueError("%s: a writable contiguous %s array of at least %d entries"
+                         % (name, np.dtype(dtype).name, points))
+
+
 class Batch:
     """Lenses (rows a, b, th, m2, m3, rho, ld_v, ppr) and trajectories
     (rows x0, y0, x1, y1) on the GPU engine."""
@@ -81,15 +119,13 @@ class Batch:
         return self.L.tlb_set_chain(self.obj, int(points))
 
     def set_lenses(self, lenses):
-        lenses = np.ascontiguousarray(lenses, np.float64)
+        lenses = _lens_rows(lenses)
         r = self.L.tlb_set_lenses(self.obj, len(lenses), lenses.ravel())
         if r < 0:
             raise RuntimeError("tlb_set_lenses failed: %d" % r)
 
     def set_trajectories(self, trajs, lens_idx, n):
-        trajs = np.ascontiguousarray(trajs, np.float64)
-        li = np.ascontiguousarray(lens_idx, np.int32)
-        nn = np.ascontiguousarray(n, np.uint32)
+        trajs, li, nn = _traj_args(trajs, lens_idx, n)
         r = self.L.tlb_set_trajectories(self.obj, len(trajs), trajs.ravel(), li, nn)
         if r < 0:
             raise RuntimeError("tlb_set_trajectories failed: %d" % r)
@@ -116,11 +152,13 @@ class Batch:
         return self.download()
 
     def run_host(self, trajs, lens_idx, n, amp, cnt, st, stream=None):
-        trajs = np.ascontiguousarray(trajs, np.float64)
-        r = self.L.tlb_run_host(self.obj, len(trajs), trajs.ravel(),
-                                np.ascontiguousarray(lens_idx, np.int32),
-                                np.ascontiguousarray(n, np.uint32), _ptr(amp), _ptr(cnt),
-                                _ptr(st), stream)
+        trajs, li, nn = _traj_args(trajs, lens_idx, n)
+        points = int(np.sum(nn.astype(np.int64) + 1))
+        _check_out("amp", amp, np.float64, points)
+        _check_out("cnt", cnt, np.uint64, points)
+        _check_out("st", st, np.uint32, points)
+        r = self.L.tlb_run_host(self.obj, len(trajs), trajs.ravel(), li, nn, _ptr(amp),
+                                _ptr(cnt), _ptr(st), stream)
         if r < 0:
             raise RuntimeError("tlb_run_host failed: %d" % r)
         self.npoints = int(r)
