@@ -1,7 +1,9 @@
-"""The batched API's Python wrapper (triplelens_gb300/batch.py) checks the
-shapes of what it hands to the C functions, which read and write as many
-rows as the counts they are given: wrong shapes raise ValueError before any
-pointer crosses the boundary.  No GPU: the checks are module functions."""
+"""The Python wrappers of the batched API (triplelens_gb300/batch.py) and of
+the reference's class (triplelens_gb300/lcirs.py) check the shapes of what
+they hand to the C functions, which read and write as many rows as the
+counts they are given: wrong shapes raise ValueError before any pointer
+crosses the boundary.  No GPU: module functions, and an LC_irs around a
+stand-in library."""
 import numpy as np
 import pytest
 
@@ -53,3 +55,40 @@ def test_output_arrays_are_checked():
     B._check_out("cnt", np.zeros(10, np.uint64), np.uint64, 10)
     with pytest.raises(ValueError):
         B._check_out("cnt", np.zeros(10, np.int64), np.uint64, 10)
+
+
+class _FakeLib:
+    """Stands in for liblcirs.so: records the calls that reach it."""
+
+    def __init__(self):
+        self.calls = []
+
+    def __getattr__(self, name):
+        def call(*args):
+            self.calls.append(name)
+        return call
+
+
+def _lc_without_gpu(n):
+    from triplelens_gb300.lcirs import LC_irs
+    lc = object.__new__(LC_irs)
+    lc.lib_lc, lc.lc_len, lc.obj = _FakeLib(), n, None
+    return lc
+
+
+def test_lc_irs_checks_sizes_before_the_c_calls():
+    """LC_irs.copy_lc writes n values and fill_from_seeds reads (n+1) x 64 x 2
+    seeds and n+1 counts (include/lcirs.h): shorter or misshapen arrays raise
+    ValueError and never reach the library."""
+    from triplelens_gb300.lcirs import MAX_SEEDS
+    lc = _lc_without_gpu(10)
+    lc.copy_lc(np.zeros(10))
+    with pytest.raises(ValueError):
+        lc.copy_lc(np.zeros(9))
+    seeds = np.zeros((11, MAX_SEEDS, 2), np.int32)
+    lc.fill_from_seeds(0.0, 0.0, 1.0, 1.0, seeds, np.zeros(11, np.int32))
+    with pytest.raises(ValueError):
+        lc.fill_from_seeds(0.0, 0.0, 1.0, 1.0, seeds[:10], np.zeros(11, np.int32))
+    with pytest.raises(ValueError):
+        lc.fill_from_seeds(0.0, 0.0, 1.0, 1.0, seeds, np.zeros(10, np.int32))
+    assert lc.lib_lc.calls == ["copy_lc", "lcirs_fill_from_seeds"]

@@ -92,6 +92,10 @@ class LC_irs(object):
         self.lib_lc.get_lc_irs(self.obj, iniX, iniY, finX, finY)
 
     def copy_lc(self, lc_vec):
+        # copy_lc writes lc_len values (lcirs.cc:566-576)
+        if isinstance(lc_vec, np.ndarray) and lc_vec.size < self.lc_len:
+            raise ValueError("copy_lc writes %d values; the array holds %d"
+                             % (self.lc_len, lc_vec.size))
         self.lib_lc.copy_lc(self.obj, lc_vec)
 
     def set_limb_darkening(self, model_type, model_parameter):
@@ -148,8 +152,13 @@ class LC_irs(object):
         return s.reshape(self.lc_len + 1, MAX_SEEDS, 2), n
 
     def fill_from_seeds(self, iniX, iniY, finX, finY, seeds, nseeds):
+        """The fill alone from given seed pixels: seeds (n+1, 64, 2) as
+        seeds() returns them, nseeds (n+1) counts (clamped to 0..64)."""
         s = np.ascontiguousarray(seeds, np.int32).reshape(-1)
-        n = np.ascontiguousarray(nseeds, np.int32)
+        n = np.ascontiguousarray(nseeds, np.int32).reshape(-1)
+        if s.size != (self.lc_len + 1) * MAX_SEEDS * 2 or n.size != self.lc_len + 1:
+            raise ValueError("fill_from_seeds: seeds of shape (%d, %d, 2) and %d counts"
+                             % (self.lc_len + 1, MAX_SEEDS, self.lc_len + 1))
         self.lib_lc.lcirs_fill_from_seeds(self.obj, iniX, iniY, finX, finY, s, n)
 
     def diag(self):
