@@ -1,11 +1,13 @@
 """Host-side logic of the surrogate (no GPU): the parameter layout of the
 initialiser agrees with the FP64 restatement's, the sampler draws the
-configured distributions, and the training-row selection keeps only clean
-IRS labels away from the caustic."""
+configured distributions, the training-row selection keeps only clean
+IRS labels away from the caustic, and the model's tensor checks reject wrong
+arguments before any launch."""
 import math
 import types
 
 import numpy as np
+import pytest
 
 
 def test_init_params_layout_matches_oracle():
@@ -59,3 +61,26 @@ def test_training_rows():
     # clean, image-count warning kept; empty IRS, table-full and near-caustic dropped
     assert list(ok) == [True, True, False, False, False]
     assert abs(y[0] - math.log(2.0 / 1.9)) < 1e-6
+
+
+def test_device_tensor_checks_reject_before_any_launch():
+    """Model methods check their device tensors (shape, type, contiguity,
+    device) and host arrays (sizes) before a kernel is told how many rows to
+    read: wrong ones raise ValueError.  On a machine without a GPU every
+    tensor is a host tensor, which is rejected too."""
+    torch = pytest.importorskip("torch")
+    from triplelens_gb300 import surrogate as S
+    feat = torch.zeros((8, S.N_FEATURES), dtype=torch.float32)
+    with pytest.raises(ValueError):
+        S._rows(feat)                                    # host tensor
+    with pytest.raises(ValueError):
+        S._rows(torch.zeros(8))                          # not 2-D
+    with pytest.raises(ValueError):
+        S._tensor("y", torch.zeros(8, dtype=torch.float64), (8,), torch.float32)
+    with pytest.raises(ValueError):
+        S._tensor("y", np.zeros(8, np.float32), (8,), torch.float32)
+    assert S._host("mean", [0.0] * S.N_FEATURES, S.N_FEATURES).dtype == np.float32
+    with pytest.raises(ValueError):
+        S._host("mean", [0.0] * 13, S.N_FEATURES)
+    with pytest.raises(ValueError):
+        S._host("params", np.zeros(10), 11)

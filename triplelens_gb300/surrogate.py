@@ -69,6 +69,35 @@ def _check(r, what):
         raise RuntimeError("%s failed: %d" % (what, r))
 
 
+# The kernels read and write as many rows as they are told: the device
+# tensors are checked here, so that a wrong shape, type or device raises
+# instead of sending a kernel past the end of a buffer.
+def _tensor(name, t, shape, dtype):
+    import torch
+    if not isinstance(t, torch.Tensor) or t.device.type != "cuda" or t.dtype != dtype \
+            or not t.is_contiguous() or tuple(t.shape) != tuple(shape):
+        raise ValueError("%s: a contiguous CUDA tensor of %s and shape %s, got %s"
+                         % (name, dtype, tuple(shape),
+                            (tuple(t.shape), t.dtype, str(t.device))
+                            if isinstance(t, torch.Tensor) else type(t).__name__))
+
+
+def _rows(feat):
+    """Rows of a feature tensor (M x N_FEATURES float32 on the GPU)."""
+    import torch
+    m = feat.shape[0] if isinstance(feat, torch.Tensor) and feat.dim() == 2 else -1
+    _tensor("feat", feat, (m, N_FEATURES), torch.float32)
+    return m
+
+
+def _host(name, a, n):
+    """A float32 host array of exactly n values, contiguous."""
+    a = np.ascontiguousarray(a, np.float32).reshape(-1)
+    if a.size != n:
+        raise ValueError("%s: %d values, got %d" % (name, n, a.size))
+    return a
+
+
 def init_params(rng, n_params):
     """He-uniform weights, zero biases, in the library's parameter layout."""
     p = np.zeros(n_params, np.float32)
@@ -110,7 +139,7 @@ class Model:
             pass
 
     def set_params(self, k, p):
-        p = np.ascontiguousarray(p, np.float32)
+        p = _host("params", p, self.n_params)
         _check(self.L.tls_set_params(self.obj, k, p.ctypes.data_as(ctypes.c_void_p)), "set_params")
 
     def get_params(self, k):
@@ -119,12 +148,14 @@ class Model:
         return p
 
     def set_normalisation(self, mean, std):
-        mean = np.ascontiguousarray(mean, np.float32)
-        std = np.ascontiguousarray(std, np.float32)
+        mean = _host("mean", mean, N_FEATURES)
+        std = _host("std", std, N_FEATURES)
         _check(self.L.tls_set_normalisation(self.obj, mean.ctypes.data_as(ctypes.c_void_p),
                                             std.ctypes.data_as(ctypes.c_void_p)), "normalisation")
 
     def gradients(self, k, feat, target):
+        import torch
+        _tensor("target", target, (_rows(feat),), torch.float32)
         g = np.zeros(self.n_params, np.float32)
         loss = np.zeros(1, np.float32)
         _check(self.L.tls_gradients(self.obj, k, feat.shape[0], _dp(feat), _dp(target),
@@ -133,17 +164,30 @@ class Model:
         return g, float(loss[0])
 
     def train_step(self, k, feat, target, lr, loss_dev=None, stream=None):
+        import torch
+        _tensor("target", target, (_rows(feat),), torch.float32)
+        if loss_dev is not None:
+            _tensor("loss_dev", loss_dev, (1,), torch.float32)
         _check(self.L.tls_train_step(self.obj, k, feat.shape[0], _dp(feat), _dp(target), lr,
                                      _dp(loss_dev) if loss_dev is not None else None, stream),
                "train_step")
 
     def forward(self, k, feat, y, stream=None):
+        import torch
+        _tensor("y", y, (_rows(feat),), torch.float32)
         _check(self.L.tls_forward(self.obj, k, feat.shape[0], _dp(feat), _dp(y), stream), "forward")
 
     def predict(self, feat, aps, dc_rho, max_std, min_dc_rho, out, far_dc_rho=GATE["far"],
                 stream=None):
         """out: dict of device tensors mean, std (float32), mag (float64),
         gated (int32)."""
+        import torch
+        m = _rows(feat)
+        _tensor("aps", aps, (m,), torch.float64)
+        _tensor("dc_rho", dc_rho, (m,), torch.float32)
+        for key, dt in (("mean", torch.float32), ("std", torch.float32), ("mag", torch.float64),
+                        ("gated", torch.int32)):
+            _tensor("out['%s']" % key, out[key], (m,), dt)
         _check(self.L.tls_predict(self.obj, feat.shape[0], _dp(feat), _dp(aps), _dp(dc_rho),
                                   float(max_std), float(min_dc_rho), float(far_dc_rho),
                                   _dp(out["mean"]),
