@@ -187,3 +187,21 @@ def test_cpp_callers_compile_and_link_against_the_class(product_lib, tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("header", ["lcirs.h", "tl_batch.h", "tl_surrogate.h", "ccc.h", "img.h",
+                                    "lccuda.h"])
+def test_headers_compile_as_c(header, tmp_path):
+    """The C-ABI headers are plain C (what a cgo, JNI or other FFI binding
+    includes): each compiles as C11 with -pedantic and no warnings."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no gcc")
+    src = tmp_path / "use.c"
+    src.write_text('#include "%s"\nint main(void) { return 0; }\n' % header)
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                        INCLUDE, "-c", str(src), "-o", str(tmp_path / "use.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
