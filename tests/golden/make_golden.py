@@ -14,7 +14,7 @@ Three reference builds (oracle/Makefile.ref): "strict" (IEEE, -O2
 show the reference's own build-to-build spread.
 
     python tests/golden/make_golden.py --ref <TripleLens checkout> [--c2] [--bench]
-        [--only-ccc | --only-bench | --only-extra]
+        [--only-ccc | --only-bench | --only-config4 | --only-extra]
 
 (--ref may be replaced by TRIPLELENS_REF in the environment.)  Each reference
 run happens in a child process of its own (its stdout is C++ cout, and its
@@ -257,6 +257,18 @@ def extra_fixtures():
     return out
 
 
+def config4_fixture(n_curves=8, n=20):
+    """Config-4 curves (each its own lens, rho log-uniform in [1e-4, 3e-2],
+    200/500/1000 rays per radius, v in [0.3, 0.7]): n + 1 points each."""
+    lenses, trajs, _ = workloads.config4(seed=5, n_curves=n_curves)
+    out = {"lenses": lenses, "trajs": trajs, "n": np.array(n)}
+    for build in ("strict", "fast"):
+        res = curves(REF_LIBS[build], lenses, trajs, n)
+        out["counts_" + build] = np.array([c for c, _ in res])
+        out["amps_" + build] = np.array([a for _, a in res])
+    return out
+
+
 def curves(lib, lenses, trajs, n):
     """Reference curves, several child processes at a time."""
     futs = [POOL.submit(run_curve, lib, lenses[k], trajs[k], n) for k in range(len(lenses))]
@@ -277,6 +289,8 @@ def main():
                     help="only the benchmark fixture (implies --bench)")
     ap.add_argument("--only-extra", action="store_true",
                     help="only extra_cases.npz (binary lens, short and far curves)")
+    ap.add_argument("--only-config4", action="store_true",
+                    help="only config4_sample.npz (config-4 lenses, radii and densities)")
     args = ap.parse_args()
     if args.worker:
         worker(json.loads(args.worker))
@@ -295,6 +309,10 @@ def main():
     if args.only_bench:
         args.bench = True
         bench_fixture()
+        return
+    np.savez_compressed(os.path.join(HERE, "config4_sample.npz"), **config4_fixture())
+    print("wrote config4_sample.npz")
+    if args.only_config4:
         return
     np.savez_compressed(os.path.join(HERE, "extra_cases.npz"), **extra_fixtures())
     print("wrote extra_cases.npz")

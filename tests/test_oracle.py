@@ -140,6 +140,22 @@ def test_extra_cases_match_reference(oracle_lib, case):
     assert np.array_equal(amps[:n], z["amps_%s_strict" % case])
 
 
+def test_config4_sample_matches_reference(oracle_lib):
+    """Config-4 curves (each its own lens; rho from 3e-4 to 2.3e-2, 200, 500
+    and 1000 rays per radius, v from 0.32 to 0.59; up to 3.2e7 rays per point):
+    counts and magnifications equal the strict reference build's on every
+    point (its -Ofast build differs from it at 7 of 168)."""
+    z = np.load(os.path.join(GOLDEN, "config4_sample.npz"))
+    n = int(z["n"])
+    for k in range(len(z["lenses"])):
+        L = z["lenses"][k]
+        o = oracle_lib.OracleIRS(*L[:5], L[5], n, int(L[7]))
+        o.set_limb_darkening("linear", L[6])
+        amps, counts = o.lc_irs(*z["trajs"][k])
+        assert np.array_equal(counts, z["counts_strict"][k]), (k, np.nonzero(counts != z["counts_strict"][k]))
+        assert np.array_equal(amps[:n], z["amps_strict"][k]), k
+
+
 def _sampled_counts(oracle_lib, L, t, n, points):
     """Counts at the given points: the whole warm-start chain (every point's
     seeds, in order), then the fill of the sampled points only."""
