@@ -1,8 +1,9 @@
 """Host-side logic of the surrogate (no GPU): the parameter layout of the
 initialiser agrees with the FP64 restatement's, the sampler draws the
 configured distributions, the training-row selection keeps only clean
-IRS labels away from the caustic, and the model's tensor checks reject wrong
-arguments before any launch."""
+IRS labels away from the caustic, the model's tensor checks reject wrong
+arguments before any launch, and the FP64 gradient restatement agrees with
+finite differences of its own loss."""
 import math
 import types
 
@@ -84,3 +85,42 @@ def test_device_tensor_checks_reject_before_any_launch():
         S._host("mean", [0.0] * 13, S.N_FEATURES)
     with pytest.raises(ValueError):
         S._host("params", np.zeros(10), 11)
+
+
+def test_gradient_oracle_matches_finite_differences(monkeypatch):
+    """The FP64 gradient restatement the GPU gradients are checked against
+    (oracle/mlp.py) is itself right: with the BF16 operand rounding switched
+    off (it makes the loss piecewise constant in the weights), its gradient
+    equals central finite differences of its loss on sampled weights and on
+    every bias and output weight."""
+    from oracle import mlp
+    monkeypatch.setattr(mlp, "bf16", lambda a: np.asarray(a, np.float64))
+    rng = np.random.Generator(np.random.PCG64(21))
+    n_params = 16 * 256 + 256 + 3 * (256 * 256 + 256) + 256 + 1
+    p = rng.normal(0.0, 0.08, n_params)
+    feat = rng.normal(0.0, 1.0, (6, 14))
+    target = rng.normal(0.0, 0.5, 6)
+    mean, std = np.zeros(14), np.ones(14)
+    _, _, g = mlp.forward_backward(p, feat, target, mean, std)
+    assert g.shape == (n_params,)
+    # a sample of weights, and every bias, output weight and the output bias
+    offs, o = [], 0
+    for fan_in in (16, 256, 256, 256):
+        o += 256 * fan_in
+        offs += list(range(o, o + 256))
+        o += 256
+    coords = np.concatenate([rng.choice(n_params, 300, replace=False), offs,
+                             np.arange(o, n_params)])
+    # inputs 14 and 15 of the first layer are padding: their weights see zeros
+    pad = [r * 16 + c for r in range(256) for c in (14, 15)]
+    assert np.all(g[pad] == 0.0)
+    h = 1e-6
+    num = np.empty(len(coords))
+    for i, c in enumerate(coords):
+        pp, pm = p.copy(), p.copy()
+        pp[c] += h
+        pm[c] -= h
+        num[i] = (mlp.forward_backward(pp, feat, target, mean, std)[0] -
+                  mlp.forward_backward(pm, feat, target, mean, std)[0]) / (2 * h)
+    scale = np.abs(g[coords]).max()
+    assert np.max(np.abs(num - g[coords])) < 1e-6 * scale
