@@ -95,7 +95,7 @@ Engine::Engine() {
   // TL_PIPE_CTAS: warp-fill CTAs per SM beside the chain (1..7)
   if (const char* c = getenv("TL_PIPE_CTAS")) pipe_ctas_ = atoi(c);
   if (const char* c = getenv("TL_TEAMS")) want_teams_ = atoi(c);
-  // TL_WFILL_CAP_LOG2: slots per warp table (10..14; the threshold follows)
+  // TL_WFILL_CAP_LOG2: slots per warp table (log2, 10..16; the threshold follows)
   if (const char* c = getenv("TL_WFILL_CAP_LOG2")) {
     wfill_cap_log2_ = atoi(c);
     if (!getenv("TL_WFILL_THR"))
