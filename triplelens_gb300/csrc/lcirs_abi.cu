@@ -64,6 +64,9 @@ namespace {
 // objects that have not run get_lc_irs yet: while there are any, a batch
 // waits longer for callers (they are likely on their way)
 std::atomic<int> g_fresh{0};
+// constructors running now (their lens set-up takes tens of ms): a batch
+// keeps gathering while there are any, within its time cap
+std::atomic<int> g_constructing{0};
 
 void setup_object(LightCurveIRS* o) {
   tl::Engine& E = tl::Engine::get();
@@ -121,8 +124,14 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
   intensityCoeff = 1.0 / (ldA + 2.0 / 3.0 * ldB);
   lcVec.assign(lcLength, 0.0);
   impl->lcFull.assign((size_t)lcLength + 1, 0.0);
+  // counted from the start of its construction until its first get_lc_irs
+  // (batching window): objects still in their lens set-up (tens of ms) when
+  // another object calls are on their way too; counted only after it, a
+  // first caller could find none and run alone
+  g_fresh.fetch_add(1);
+  g_constructing.fetch_add(1);
   setup_object(this);
-  g_fresh.fetch_add(1);   // until its first get_lc_irs (batching window)
+  g_constructing.fetch_sub(1);
 }
 
 LightCurveIRS::~LightCurveIRS() {
@@ -258,8 +267,9 @@ void absorb_results(LightCurveIRS* o, std::complex<double> s, std::complex<doubl
 // their own launches from different host threads mostly wait for each
 // other.  Instead, a call queues its request; the first caller that finds no
 // batch running becomes the leader, waits until requests stop arriving (a
-// gap of 3 ms, 15 ms while objects exist that have not called yet; at most
-// 300 ms), and runs every queued request with its chain and precision
+// gap of 3 ms, 15 ms while objects exist that have not called yet, and no
+// object still in its constructor; at most 300 ms), and runs every queued
+// request with its chain and precision
 // settings as one batch: the seeds (a chain per curve; the exact chain in
 // segments overlapped with the fill) and the fill, on the batcher's stream.
 // Every caller then finds its results in its object, exactly as a lone call
@@ -432,13 +442,14 @@ void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
     if (!B.running) {
       B.running = true;
       // gather callers: until a quiet gap of 3 ms (15 ms while objects that
-      // have not called yet exist), at most 300 ms
+      // have not called yet exist) with no constructor running, at most
+      // 300 ms
       const auto t0 = std::chrono::steady_clock::now();
       uint64_t seen = B.arrivals;
       for (;;) {
         const int gap = g_fresh.load() > 0 ? 15 : 3;
         B.cv.wait_for(lk, std::chrono::milliseconds(gap));
-        if (B.arrivals == seen ||
+        if ((B.arrivals == seen && g_constructing.load() == 0) ||
             std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(300))
           break;
         seen = B.arrivals;
