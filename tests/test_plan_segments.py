@@ -5,7 +5,9 @@ point is listed exactly once, each curve's segments are consecutive shares
 in order with the curve as their chain, and the counts and offsets agree.
 The seeds of a segmented chain equal one unbroken chain only if these hold
 (the GPU tests check the seeds themselves).  The same header holds the
-autotuner's choice among its timed candidates, tested here on set timings."""
+autotuner's choice among its timed candidates, tested here on set timings,
+and the object batcher's gathering of concurrent callers, run here in threads
+with emulated lens set-ups."""
 import os
 import shutil
 import subprocess
@@ -99,6 +101,101 @@ int main() {
 """
 
 
+GATHER = r"""
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <mutex>
+#include <thread>
+#include <vector>
+#include "plan.h"
+
+// the object batcher's structure (lcirs_abi.cu runBatched): requests queue,
+// the first caller with no batch running leads, gathers, runs the batch
+struct Sim {
+  std::mutex mu;
+  std::condition_variable cv;
+  uint64_t arrivals = 0;
+  std::vector<int*> pending;
+  bool running = false;
+  std::vector<size_t> batches;
+  std::atomic<int> fresh{0}, constructing{0};
+
+  void construct(int ms) {
+    fresh++;
+    constructing++;
+    std::this_thread::sleep_for(std::chrono::milliseconds(ms));   // lens set-up
+    constructing--;
+  }
+  void call(int run_ms) {
+    int done = 0;
+    std::unique_lock<std::mutex> lk(mu);
+    fresh--;
+    pending.push_back(&done);
+    arrivals++;
+    cv.notify_all();
+    while (!done) {
+      if (!running) {
+        running = true;
+        tl::gather_callers(lk, cv, arrivals, fresh, constructing);
+        std::vector<int*> mine;
+        mine.swap(pending);
+        batches.push_back(mine.size());
+        lk.unlock();
+        std::this_thread::sleep_for(std::chrono::milliseconds(run_ms));   // the batch
+        lk.lock();
+        for (int* d : mine) *d = 1;
+        running = false;
+        cv.notify_all();
+      } else {
+        cv.wait(lk);
+      }
+    }
+  }
+};
+
+int main() {
+  using clk = std::chrono::steady_clock;
+  // 152 objects created and called from a pool of threads, the first
+  // object's set-up ending 10 ms before the others': one batch
+  for (int rep = 0; rep < 3; rep++) {
+    Sim s;
+    std::vector<std::thread> th;
+    for (int k = 0; k < 152; k++)
+      th.emplace_back([&s, k] { s.construct(k == 0 ? 22 : 32); s.call(20); });
+    for (auto& t : th) t.join();
+    if (s.batches.size() != 1 || s.batches[0] != 152) {
+      printf("FAIL pool: %zu batches, first %zu\n", s.batches.size(), s.batches[0]);
+      return 1;
+    }
+  }
+  // a lone caller waits one short gap, not the cap
+  {
+    Sim s;
+    s.construct(1);
+    const auto t0 = clk::now();
+    s.call(0);
+    const double ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    if (ms > 100.0) { printf("FAIL lone caller waited %.1f ms\n", ms); return 1; }
+  }
+  // a constructor that does not end soon: the cap closes the gathering
+  {
+    Sim s;
+    std::thread slow([&s] { s.construct(1500); });
+    std::this_thread::sleep_for(std::chrono::milliseconds(5));
+    s.construct(1);
+    const auto t0 = clk::now();
+    s.call(0);
+    const double ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    slow.join();
+    if (ms < 250.0 || ms > 1000.0) { printf("FAIL cap: %.1f ms\n", ms); return 1; }
+  }
+  printf("OK\n");
+  return 0;
+}
+"""
+
+
 def _compile_and_run(tmp_path, name, program):
     gxx = shutil.which("g++")
     if not gxx:
@@ -106,8 +203,9 @@ def _compile_and_run(tmp_path, name, program):
     src = tmp_path / (name + ".cc")
     src.write_text(program)
     exe = tmp_path / name
-    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "triplelens_gb300", "csrc"),
-                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-pthread", "-I",
+                        os.path.join(ROOT, "triplelens_gb300", "csrc"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
@@ -121,3 +219,13 @@ def test_autotuner_keeps_the_default_unless_the_fastest_beats_it_by_5_percent(tm
     """tlb_autotune's choice among its five fill-stage candidates
     (triplelens_gb300/csrc/batch_abi.cu) through tl::pick_candidate."""
     _compile_and_run(tmp_path, "pick_test", PICK)
+
+
+def test_batcher_gathers_callers_whose_constructors_are_still_running(tmp_path):
+    """The object batcher's gathering (tl::gather_callers, used by
+    lcirs_abi.cu) in threads on the CPU: 152 callers whose first object's
+    set-up ends 10 ms before the others' form one batch (counting objects
+    only after their constructor split them 1 + 151); a lone caller waits
+    a short gap; a constructor that does not end is cut off by the 300 ms
+    cap."""
+    _compile_and_run(tmp_path, "gather_test", GATHER)

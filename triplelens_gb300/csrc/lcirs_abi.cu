@@ -444,16 +444,7 @@ void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
       // gather callers: until a quiet gap of 3 ms (15 ms while objects that
       // have not called yet exist) with no constructor running, at most
       // 300 ms
-      const auto t0 = std::chrono::steady_clock::now();
-      uint64_t seen = B.arrivals;
-      for (;;) {
-        const int gap = g_fresh.load() > 0 ? 15 : 3;
-        B.cv.wait_for(lk, std::chrono::milliseconds(gap));
-        if ((B.arrivals == seen && g_constructing.load() == 0) ||
-            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(300))
-          break;
-        seen = B.arrivals;
-      }
+      tl::gather_callers(lk, B.cv, B.arrivals, g_fresh, g_constructing);
       std::vector<Request*> mine, rest;
       for (Request* q : B.pending)
         (q->chain == r.chain && q->precision == r.precision ? mine : rest).push_back(q);

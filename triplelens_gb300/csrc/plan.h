@@ -1,6 +1,7 @@
 // plan.h - host-side planning (no CUDA; included by the batched API and the
 // object batcher, and compiled alone by the CPU tests): the exact warm-start
-// chain in segments, and the autotuner's choice among timed candidates.
+// chain in segments, the autotuner's choice among timed candidates, and the
+// object batcher's gathering of concurrent callers.
 //
 // Segments: every curve's n+1 points are cut into nseg consecutive shares of
 // ceil((n+1)/nseg) points (the last shares of a short curve may be empty).
@@ -12,6 +13,8 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <vector>
 
 namespace tl {
@@ -65,6 +68,27 @@ inline int pick_candidate(const float* ms, int n, float margin) {
   if (best < 0) return 0;
   if (ms[0] > 0.f && ms[best] >= (1.f - margin) * ms[0]) return 0;
   return best;
+}
+
+// The object batcher's gathering of concurrent callers (called by the
+// leader with `lk` held on the mutex `cv` waits with): waits until requests
+// stop arriving - a quiet gap of 3 ms, 15 ms while objects exist that have
+// not called yet (`fresh`), with no object still in its constructor
+// (`constructing`) - or max_ms have passed.  `arrivals` counts requests and
+// is read under the lock.
+template <class Lock, class Cv>
+void gather_callers(Lock& lk, Cv& cv, const uint64_t& arrivals, const std::atomic<int>& fresh,
+                    const std::atomic<int>& constructing, int max_ms = 300) {
+  const auto t0 = std::chrono::steady_clock::now();
+  uint64_t seen = arrivals;
+  for (;;) {
+    const int gap = fresh.load() > 0 ? 15 : 3;
+    cv.wait_for(lk, std::chrono::milliseconds(gap));
+    if ((arrivals == seen && constructing.load() == 0) ||
+        std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(max_ms))
+      break;
+    seen = arrivals;
+  }
 }
 
 }  // namespace tl
