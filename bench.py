@@ -269,6 +269,7 @@ def config4_leg(seed, curves, reps):
     ms_plain = e0.elapsed_time(e1)
     _, cnt, st = b.download(stream.cuda_stream)
     stats = b.stats()
+    parity = config4_fixture_parity()
     return {"workload": "config 4 sub-sample: %d curves x %d points, own lens each" % (curves, n + 1),
             "points": int(npts), "ms_per_replay": ms_graph, "points_per_s": npts / (ms_graph / 1e3),
             "rays_evaluated_per_s": float(stats[0]) / (ms_graph / 1e3),
@@ -284,7 +285,29 @@ def config4_leg(seed, curves, reps):
             "status_or": int(np.bitwise_or.reduce(st)),
             # points whose magnification is incomplete (table full or a wait ran out)
             "incomplete_points": int(((st & 0xC) != 0).sum()),
-            "status_counts": status_counts(st)}
+            "status_counts": status_counts(st),
+            "parity_vs_reference_fixture": parity}
+
+
+def config4_fixture_parity():
+    """Ray counts of the reference's strict build on 8 config-4 curves x 21
+    points (tests/golden/config4_sample.npz: radii 3e-4 to 2e-2, 200 to 1000
+    rays per radius) against the engine's (exact chain), reported rather
+    than asserted."""
+    from triplelens_gb300.batch import Batch
+    try:
+        z = np.load(os.path.join(ROOT, "tests", "golden", "config4_sample.npz"))
+        n, lenses, trajs = int(z["n"]), z["lenses"], z["trajs"]
+        b = Batch()
+        b.set_chain(0)
+        b.set_lenses(lenses)
+        _, cnt, st = b.run(trajs, np.arange(len(trajs)), n)
+        ref = z["counts_strict"].ravel()
+        return {"points": int(len(ref)), "mismatches": int(np.sum(cnt != ref)),
+                "incomplete_points": int(((st & 0xC) != 0).sum()),
+                "fixture": "tests/golden/config4_sample.npz (the reference's strict build)"}
+    except Exception as e:   # reported, never fatal to the leg
+        return {"error": repr(e)[:300]}
 
 
 def surrogate_leg(seed, train_lenses, eval_lenses):
