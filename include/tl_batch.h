@@ -87,9 +87,10 @@ long tlb_point_lc(tl_batch* b, double* amp);
  * 32 x 32 rays): one warp per point up to 7000, 3000 or 1500 blocks and a
  * team of 8 warps per larger point; one warp up to 7000 and the CTA fill for
  * larger points; the CTA fill alone.  Keeps the fastest for later runs of the
- * process (the first, the default, unless another is 5 % faster).  chosen3 = {warp-fill threshold in blocks (0: CTA fill alone),
- * 1 if the team fill takes the larger points, points timed}; times_ms (5
- * floats, may be NULL) the fill times in that order.  Results do not depend
+ * process if it beats the first (the default) by more than 5 %, else the
+ * default.  chosen3 = {warp-fill threshold in blocks (0: CTA fill alone), 1 if
+ * the team fill takes the larger points, points timed}; times_ms (5 floats,
+ * may be NULL) the fill times in that order.  Results do not depend
  * on the choice (the filled sets are exact). */
 int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times_ms);
 

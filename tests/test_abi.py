@@ -205,3 +205,20 @@ def test_headers_compile_as_c(header, tmp_path):
                         INCLUDE, "-c", str(src), "-o", str(tmp_path / "use.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_guide_names_every_entry_point():
+    """INTEGRATION.md names every function include/*.h declares, so a
+    maintainer binding the libraries (ctypes, cgo, JNI) finds each one."""
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        guide = f.read()
+    missing = []
+    for h in sorted(os.listdir(INCLUDE)):
+        if not h.endswith(".h"):
+            continue
+        with open(os.path.join(INCLUDE, h)) as f:
+            src = f.read()
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(\w+)\s*\(", src, re.M):
+            if m.group(1) not in guide:
+                missing.append((h, m.group(1)))
+    assert not missing, missing
