@@ -124,3 +124,31 @@ def test_gradient_oracle_matches_finite_differences(monkeypatch):
                   mlp.forward_backward(pm, feat, target, mean, std)[0]) / (2 * h)
     scale = np.abs(g[coords]).max()
     assert np.max(np.abs(num - g[coords])) < 1e-6 * scale
+
+
+def test_checkpoint_round_trip_and_rejections(tmp_path):
+    """Surrogate checkpoints (flat binary with a header): a round trip keeps
+    every parameter, the standardisation and the metadata bit for bit; other
+    files, bad headers and short files raise ValueError."""
+    from triplelens_gb300 import surrogate as S
+    rng = np.random.Generator(np.random.PCG64(3))
+    params = rng.normal(0.0, 1.0, (4, 1000)).astype(np.float32)
+    mean = rng.normal(0.0, 1.0, S.N_FEATURES).astype(np.float32)
+    std = rng.uniform(0.5, 2.0, S.N_FEATURES).astype(np.float32)
+    path = tmp_path / "model.tls"
+    S.save_checkpoint(path, params, mean, std, {"gate": S.GATE, "train_points": 55000})
+    p2, m2, s2, meta = S.load_checkpoint(path)
+    assert p2.dtype == np.float32 and np.array_equal(p2, params)
+    assert np.array_equal(m2, mean) and np.array_equal(s2, std)
+    assert meta == {"gate": S.GATE, "train_points": 55000}
+    raw = path.read_bytes()
+    bad = tmp_path / "bad"
+    for content in (b"not a checkpoint at all......", raw[:-4], raw + b"\0\0\0\0",
+                    raw[:8] + np.array([4, 1000, 13, 0], "<i4").tobytes() + raw[24:]):
+        bad.write_bytes(content)
+        with pytest.raises(ValueError):
+            S.load_checkpoint(bad)
+    with pytest.raises(ValueError):
+        S.save_checkpoint(path, params[0], mean, std)          # one row per member
+    with pytest.raises(ValueError):
+        S.save_checkpoint(path, params, mean[:10], std)

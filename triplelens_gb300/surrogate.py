@@ -117,6 +117,52 @@ def init_params(rng, n_params):
     return p
 
 
+CHECKPOINT_MAGIC = b"TLSURR01"
+
+
+def save_checkpoint(path, params, mean, std, meta=None):
+    """Writes an ensemble as a flat binary with a header: the 8-byte magic,
+    four little-endian int32 (members, parameters per member, features,
+    metadata bytes), the metadata (UTF-8 JSON), then float32 arrays: the
+    feature mean and standard deviation, and every member's parameters in
+    the library's layout.  Adam's moments are not kept: tls_set_params
+    starts them from zero, so training resumes with fresh moments."""
+    import json
+    params = np.ascontiguousarray(params, np.float32)
+    if params.ndim != 2:
+        raise ValueError("params: one row per member")
+    mean = _host("mean", mean, N_FEATURES)
+    std = _host("std", std, N_FEATURES)
+    blob = json.dumps(meta or {}).encode()
+    head = np.array([params.shape[0], params.shape[1], N_FEATURES, len(blob)], "<i4")
+    with open(path, "wb") as f:
+        f.write(CHECKPOINT_MAGIC)
+        f.write(head.tobytes())
+        f.write(blob)
+        for a in (mean, std, params):
+            f.write(a.astype("<f4").tobytes())
+
+
+def load_checkpoint(path):
+    """(params (members x n), mean, std, meta) from save_checkpoint's file;
+    ValueError on another format or a short file."""
+    import json
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:8] != CHECKPOINT_MAGIC or len(data) < 24:
+        raise ValueError("%s: not a surrogate checkpoint" % path)
+    members, n, nf, nmeta = (int(x) for x in np.frombuffer(data[8:24], "<i4"))
+    if members <= 0 or n <= 0 or nf != N_FEATURES or nmeta < 0:
+        raise ValueError("%s: bad header" % path)
+    o = 24 + nmeta
+    need = o + 4 * (2 * nf + members * n)
+    if len(data) != need:
+        raise ValueError("%s: %d bytes, the header says %d" % (path, len(data), need))
+    meta = json.loads(data[24:o].decode() or "{}")
+    floats = np.frombuffer(data[o:], "<f4").astype(np.float32)
+    return floats[2 * nf:].reshape(members, n), floats[:nf], floats[nf:2 * nf], meta
+
+
 class Model:
     """Ensemble of MLPs in the library (BF16 GEMMs, FP32 Adam)."""
 
@@ -128,6 +174,9 @@ class Model:
         if not self.obj:
             raise RuntimeError("tls_new failed")
         self.n_params = self.L.tls_param_count()
+        # the library's initial standardisation (identity)
+        self.mean = np.zeros(N_FEATURES, np.float32)
+        self.std = np.ones(N_FEATURES, np.float32)
         rng = np.random.Generator(np.random.PCG64(seed))
         for k in range(members):
             self.set_params(k, init_params(rng, self.n_params))
@@ -152,6 +201,25 @@ class Model:
         std = _host("std", std, N_FEATURES)
         _check(self.L.tls_set_normalisation(self.obj, mean.ctypes.data_as(ctypes.c_void_p),
                                             std.ctypes.data_as(ctypes.c_void_p)), "normalisation")
+        self.mean, self.std = mean.copy(), std.copy()
+
+    def save(self, path, meta=None):
+        """The ensemble's weights and standardisation (save_checkpoint)."""
+        save_checkpoint(path, np.stack([self.get_params(k) for k in range(self.members)]),
+                        self.mean, self.std, meta)
+
+    @classmethod
+    def load(cls, path, lib=None):
+        """An ensemble from save_checkpoint's file, and its metadata."""
+        params, mean, std, meta = load_checkpoint(path)
+        m = cls(members=params.shape[0], lib=lib)
+        if params.shape[1] != m.n_params:
+            raise ValueError("%s: %d parameters per member, the library has %d"
+                             % (path, params.shape[1], m.n_params))
+        for k in range(m.members):
+            m.set_params(k, params[k])
+        m.set_normalisation(mean, std)
+        return m, meta
 
     def gradients(self, k, feat, target):
         import torch
