@@ -94,6 +94,14 @@ long tlb_point_lc(tl_batch* b, double* amp);
  * on the choice (the filled sets are exact). */
 int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times_ms);
 
+/* Sets how the fill's stages share the points, as tlb_autotune chooses (to
+ * reapply a saved choice): warp_threshold_blocks > 0 sends each point up to
+ * that many predicted blocks of 32 x 32 rays to one warp and larger points
+ * to the team fill (team != 0) or the CTA fill; 0 sends every point to the
+ * CTA fill.  Process-wide, like the autotuner's choice; results do not
+ * depend on it.  -1 on a negative threshold. */
+int tlb_set_fill_stages(tl_batch* b, int warp_threshold_blocks, int team);
+
 /* Captures seeds + fill of the current trajectories (one warm run first,
  * so the captured run allocates nothing) into a CUDA graph on the engine's
  * stream.  tlb_graph_launch replays it on `stream` (NULL: the engine's);

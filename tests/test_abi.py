@@ -90,7 +90,8 @@ def test_entry_points_reject_bad_arguments_without_a_gpu(product_lib):
     f.restype = ctypes.c_int
     assert f(None, 10, None, None, None, None, None, None, None) == -1
     for name, args in (("tlb_run_device", [None, 3, None]), ("tlb_stats", [None, None]),
-                       ("tlb_graph_launch", [None, None]), ("tlb_graph_capture", [None])):
+                       ("tlb_graph_launch", [None, None]), ("tlb_graph_capture", [None]),
+                       ("tlb_set_fill_stages", [None, 7000, 1])):
         fn = getattr(lib, name)
         fn.restype = ctypes.c_int
         fn.argtypes = [vp if not isinstance(a, int) else ctypes.c_int for a in args]

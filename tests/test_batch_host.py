@@ -92,3 +92,18 @@ def test_lc_irs_checks_sizes_before_the_c_calls():
     with pytest.raises(ValueError):
         lc.fill_from_seeds(0.0, 0.0, 1.0, 1.0, seeds, np.zeros(10, np.int32))
     assert lc.lib_lc.calls == ["copy_lc", "lcirs_fill_from_seeds"]
+
+
+def test_tuning_json_round_trip(tmp_path):
+    """The autotuner's choice saved as JSON (batch.save_tuning) comes back
+    as (warp-fill threshold, team) for Batch.set_fill_stages."""
+    path = tmp_path / "tuning.json"
+    B.save_tuning(path, (3000, 1, 32768), [420.0, 401.5, 430.0, 431.0, 457.0], {"gpu": "x"})
+    assert B.load_tuning(path) == (3000, True)
+    import json
+    d = json.loads(path.read_text())
+    assert d["candidates_ms"]["warp<=3000+team"] == 401.5 and d["points_timed"] == 32768
+    B.save_tuning(path, (0, 0, 10))
+    assert B.load_tuning(path) == (0, False)
+    with pytest.raises(ValueError):
+        B.save_tuning(path, (-1, 0, 10))

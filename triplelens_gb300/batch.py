@@ -41,6 +41,8 @@ def _bind(L):
     L.tlb_set_chain.restype = ctypes.c_int
     L.tlb_point_lc.argtypes = [vp, f64]
     L.tlb_point_lc.restype = ctypes.c_long
+    L.tlb_set_fill_stages.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.tlb_set_fill_stages.restype = ctypes.c_int
     L.tlb_autotune.argtypes = [vp, ctypes.c_long, ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"),
                                ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")]
     L.tlb_autotune.restype = ctypes.c_int
@@ -182,6 +184,12 @@ class Batch:
             raise RuntimeError("tlb_autotune failed: %d" % r)
         return tuple(int(x) for x in chosen), times
 
+    def set_fill_stages(self, warp_threshold_blocks, team):
+        """Reapplies a choice of tlb_autotune (see save_tuning/load_tuning)."""
+        r = self.L.tlb_set_fill_stages(self.obj, int(warp_threshold_blocks), int(team))
+        if r < 0:
+            raise RuntimeError("tlb_set_fill_stages failed: %d" % r)
+
     def graph_capture(self):
         r = self.L.tlb_graph_capture(self.obj)
         if r < 0:
@@ -198,3 +206,35 @@ class Batch:
         if r < 0:
             raise RuntimeError("tlb_point_lc failed: %d" % r)
         return amp
+
+
+# The autotuner's choice as JSON, so that a later process can apply it without
+# timing again (Batch.set_fill_stages).
+CANDIDATES = ("warp<=7000+team", "warp<=3000+team", "warp<=1500+team", "warp<=7000+cta", "cta")
+
+
+def save_tuning(path, chosen, times_ms=None, meta=None):
+    """Writes (warp-fill threshold, team, points timed) of Batch.autotune and
+    its candidate timings to a JSON file."""
+    import json
+    thr, team, points = (int(x) for x in chosen)
+    if thr < 0:
+        raise ValueError("warp-fill threshold must be >= 0")
+    out = {"warp_fill_threshold_blocks": thr, "team_fill": bool(team), "points_timed": points}
+    if times_ms is not None:
+        out["candidates_ms"] = {k: float(t) for k, t in zip(CANDIDATES, times_ms)}
+    if meta:
+        out["meta"] = meta
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+
+
+def load_tuning(path):
+    """(warp-fill threshold, team) from save_tuning's file."""
+    import json
+    with open(path) as f:
+        d = json.load(f)
+    thr = int(d["warp_fill_threshold_blocks"])
+    if thr < 0:
+        raise ValueError("%s: negative warp-fill threshold" % path)
+    return thr, bool(d["team_fill"])

@@ -354,6 +354,15 @@ int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times
   return 0;
 }
 
+int tlb_set_fill_stages(tl_batch* b, int warp_threshold_blocks, int team) {
+  if (!b || warp_threshold_blocks < 0) return -1;
+  tl::Engine& E = tl::Engine::get();
+  std::lock_guard<std::mutex> g(E.mu);
+  const bool warp = warp_threshold_blocks > 0;
+  E.set_fill_paths(warp, warp && team != 0, (unsigned)warp_threshold_blocks);
+  return 0;
+}
+
 int tlb_graph_capture(tl_batch* b) {
   if (!b || b->npoints <= 0) return -1;
   tl::Engine& E = tl::Engine::get();
