@@ -25,7 +25,11 @@ typedef struct LightCurveIRS LightCurveIRS;
 /* Replaces lcirs_new (src/LightCurves/lcirs.cc:517-537).  Lens a, b, th, m2,
  * m3 (z1 = 0, z2 = (a,0), z3 = b e^{i th}, m1 = 1 - m2 - m3), source radius,
  * light-curve length n, rays per source radius.  Computes the critical curve,
- * caustics and image-plane grid on the GPU. */
+ * caustics and image-plane grid on the GPU.  With parameters the set-up
+ * cannot use (a non-finite value, a source radius <= 0, rays per radius
+ * outside 1..2^31-1) the object is still returned but never reaches the GPU:
+ * lcirs_last_status reads 32 (bad input), and every curve it computes has
+ * zero counts and magnifications with status 32 on every point. */
 LightCurveIRS* lcirs_new(double a, double b, double th, double m2, double m3, double sourceSize,
                          unsigned int lcLength, long pointsPerRadius);
 

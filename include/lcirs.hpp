@@ -98,6 +98,9 @@ struct LightCurveIRS {
   // getLCIRS without the amoeba dump: joins concurrent calls of other objects
   // into one launch (same results as runFill)
   void runBatched(std::complex<double> s, std::complex<double> e);
+  // results of an object whose parameters the lens set-up cannot use: zero
+  // counts and magnifications, status bit 32 on every point
+  void badInputResults();
 
  private:
   // A, B and the intensity coefficient into the object and its device lens;

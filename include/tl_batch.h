@@ -34,7 +34,9 @@ typedef struct tl_batch tl_batch;
 tl_batch* tlb_new(void);
 void tlb_delete(tl_batch* b);
 
-/* Lens set-up on the GPU (critical curves, caustics, grids). */
+/* Lens set-up on the GPU (critical curves, caustics, grids).  -1, before
+ * any GPU work, if a row holds a non-finite value, rho <= 0 or rays per
+ * radius outside 1..2^31-1. */
 int tlb_set_lenses(tl_batch* b, int nlens, const double* params8);
 
 /* Uploads trajectories (host arrays) into device memory and plans the

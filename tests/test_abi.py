@@ -223,3 +223,36 @@ def test_integration_guide_names_every_entry_point():
             if m.group(1) not in guide:
                 missing.append((h, m.group(1)))
     assert not missing, missing
+
+
+@pytest.mark.parametrize("bad", [
+    dict(rho=float("nan")), dict(rho=0.0), dict(rho=-1e-3), dict(ppr=0),
+    dict(a=float("inf")), dict(m2=float("nan"))])
+def test_bad_lens_parameters_come_back_as_status(product_lib, bad):
+    """Lens parameters the set-up cannot use (non-finite values, rho <= 0,
+    ppr < 1): lcirs_new still returns an object, as the reference's does, but
+    it never reaches the GPU; every call leaves zero results and status bit
+    32 (bad input) on every point.  Runs without a GPU for that reason."""
+    import numpy as np
+    from triplelens_gb300.lcirs import LC_irs, MAX_SEEDS
+    p = dict(a=1.0, b=0.9, th=1.0, m2=0.2, m3=0.1, rho=1e-3, n=20, ppr=100)
+    p.update(bad)
+    lc = LC_irs(p["a"], p["b"], p["th"], p["m2"], p["m3"], p["rho"], p["n"], p["ppr"],
+                lib_path=product_lib)
+    assert lc.last_status() == 32
+    lc.set_limb_darkening("linear", 0.5)
+    lc.get_lc_irs(-1.0, 0.0, 1.0, 0.1)
+    assert lc.last_status() == 32
+    assert np.all(lc.status() == 32) and np.all(lc.counts() == 0)
+    out = np.full(p["n"], -1.0)
+    lc.copy_lc(out)
+    assert np.all(out == 0.0)
+    lc.get_lc(-1.0, 0.0, 1.0, 0.1)
+    lc.copy_lc(out)
+    assert np.all(out == 0.0) and lc.last_status() == 32
+    seeds = np.zeros((p["n"] + 1, MAX_SEEDS, 2), np.int32)
+    lc.fill_from_seeds(-1.0, 0.0, 1.0, 0.1, seeds, np.full(p["n"] + 1, 3, np.int32))
+    assert np.all(lc.status() == 32) and np.all(lc.lc_full() == 0.0)
+    # no image plane (the amplitude scale, grid[6], follows set_limb_darkening)
+    assert np.all(lc.grid()[[0, 1, 2, 3, 4, 5, 7]] == 0.0)
+    del lc

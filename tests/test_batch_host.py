@@ -19,6 +19,12 @@ def test_lens_rows():
     for bad in ([1.0, 2.0], np.zeros((2, 7)), np.zeros((0, 8)), np.zeros((2, 8, 1))):
         with pytest.raises(ValueError):
             B._lens_rows(bad)
+    # rows the lens set-up cannot use
+    for k, v in ((5, 0.0), (5, -1e-3), (5, np.nan), (7, 0.0), (0, np.inf), (3, np.nan)):
+        row = np.array(one)
+        row[k] = v
+        with pytest.raises(ValueError):
+            B._lens_rows(np.stack([np.array(one), row]))
 
 
 def test_traj_args_broadcast_and_check():

@@ -66,6 +66,11 @@ def _lens_rows(lenses):
     if a.ndim != 2 or a.shape[1] != 8 or a.shape[0] == 0:
         raise ValueError("lenses: rows of 8 values (a, b, th, m2, m3, rho, ld_v, ppr), "
                          "got shape %s" % (a.shape,))
+    bad = ~np.all(np.isfinite(a), axis=1) | ~(a[:, 5] > 0) | ~(a[:, 7] >= 1) | \
+        ~(a[:, 7] <= 2 ** 31 - 1)
+    if np.any(bad):
+        raise ValueError("lenses: rows %s have non-finite values, rho <= 0 or rays per "
+                         "radius outside 1..2^31-1" % np.nonzero(bad)[0][:10].tolist())
     return a
 
 

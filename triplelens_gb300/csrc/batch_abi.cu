@@ -55,6 +55,14 @@ void tlb_delete(tl_batch* b) {
 
 static int set_lenses_body(tl_batch* b, int nlens, const double* p8) {
   if (!b || nlens <= 0 || !p8) return -1;
+  // rows the lens set-up cannot use (as lcirs_new's bad input): non-finite
+  // values, rho <= 0, rays per radius outside 1..2^31-1
+  for (int i = 0; i < nlens; i++) {
+    const double* q = p8 + 8 * (size_t)i;
+    for (int k = 0; k < 8; k++)
+      if (!std::isfinite(q[k])) return -1;
+    if (!(q[5] > 0.0) || q[7] < 1.0 || q[7] > 2147483647.0) return -1;
+  }
   tl::Engine& E = tl::Engine::get();
   std::lock_guard<std::mutex> g(E.mu);
   std::vector<tl::LensSpec> specs(nlens);

@@ -49,6 +49,9 @@ struct LightCurveIRS::Impl {
   tl::DevBuf specbuf, ampbuf;
   bool failed = false;
   bool fresh = true;        // no get_lc_irs yet
+  // parameters the lens set-up cannot use: the object runs nothing on the
+  // GPU and its calls report status bit 32 (bad input)
+  bool invalid = false;
   bool ck(cudaError_t e) {
     if (e != cudaSuccess) {
       fprintf(stderr, "liblcirs: CUDA error %s\n", cudaGetErrorString(e));
@@ -124,6 +127,19 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
   intensityCoeff = 1.0 / (ldA + 2.0 / 3.0 * ldB);
   lcVec.assign(lcLength, 0.0);
   impl->lcFull.assign((size_t)lcLength + 1, 0.0);
+  for (double& g : grid) g = 0.0;
+  // a non-finite parameter, a source radius <= 0 or a ray density outside
+  // 1..2^31-1 would give the lens set-up no usable grid (the reference's
+  // arithmetic is undefined there): such an object exists, as the
+  // reference's does, but never reaches the GPU
+  if (!(std::isfinite(a_) && std::isfinite(b_) && std::isfinite(th_) && std::isfinite(m2_) &&
+        std::isfinite(m3_) && std::isfinite(sourceSize) && sourceSize > 0.0 && ppr >= 1 &&
+        ppr <= 2147483647L)) {
+    impl->invalid = true;
+    impl->fresh = false;
+    lastStatus = tl::kStBadInput;
+    return;
+  }
   // counted from the start of its construction until its first get_lc_irs
   // (batching window): objects still in their lens set-up (tens of ms) when
   // another object calls are on their way too; counted only after it, a
@@ -135,7 +151,7 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
 }
 
 LightCurveIRS::~LightCurveIRS() {
-  tl::Engine::get().trace("delete object");
+  if (impl && !impl->invalid) tl::Engine::get().trace("delete object");
   if (impl && impl->fresh) g_fresh.fetch_sub(1);
   if (impl) {
     // stream-ordered releases: no wait for work on other streams
@@ -156,7 +172,7 @@ LightCurveIRS::~LightCurveIRS() {
 }
 
 void LightCurveIRS::setLimbDarkening(const std::string& model, double v) {
-  tl::Engine::get().trace("setLimbDarkening");
+  if (!impl->invalid) tl::Engine::get().trace("setLimbDarkening");
   // limbdarkeningmodel.cc:18-28 ("linear") and 8-15 (anything else)
   setLimbDarkeningModel(model == "linear" ? LimbDarkeningModel(v) : LimbDarkeningModel());
 }
@@ -178,6 +194,7 @@ void LightCurveIRS::applyLimbDarkening(double A, double B, double intensity) {
   impl->spec.ld_a = ldA;
   impl->spec.ld_b = ldB;
   impl->spec.intensity = intensityCoeff;
+  if (impl->invalid) return;   // no device lens
   impl->ck(tl::copy_async(impl->d_lens, &impl->lens, sizeof(tl::DevLens), cudaMemcpyHostToDevice,
                            impl->st));
   impl->ck(cudaStreamSynchronize(impl->st));
@@ -476,8 +493,25 @@ void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
   }
 }
 
+void LightCurveIRS::badInputResults() {
+  const size_t np = (size_t)lcLength + 1;
+  counts.assign(np, 0);
+  status.assign(np, tl::kStBadInput);
+  diag.assign(np, 0);
+  nseeds.assign(np, 0);
+  seeds.assign(np * 2 * tl::kMaxSeeds, 0);
+  for (double& v : lcVec) v = 0.0;
+  for (double& v : impl->lcFull) v = 0.0;
+  stats[0] = stats[1] = stats[2] = 0;
+  lastStatus = tl::kStBadInput;
+}
+
 void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
                             const int32_t* extSeeds, const int32_t* extN) {
+  if (impl->invalid) {
+    badInputResults();
+    return;
+  }
   tl::Engine& E = tl::Engine::get();
   auto* I = impl;
   I->failed = false;
@@ -610,6 +644,10 @@ void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
     impl->fresh = false;
     g_fresh.fetch_sub(1);
   }
+  if (impl->invalid) {
+    badInputResults();
+    return;
+  }
   if (amoebaPrintOut_) {
     printOutLCParameters();
     runFill(s, e, nullptr, nullptr);   // the amoeba dump needs the object's own run
@@ -621,6 +659,12 @@ void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
 void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   auto* I = impl;
   const uint32_t n = lcLength;
+  if (I->invalid) {
+    for (double& v : lcVec) v = 0.0;
+    for (double& v : I->lcFull) v = 0.0;
+    lastStatus = tl::kStBadInput;
+    return;
+  }
   if (n == 0) return;
   tl::Traj T;
   T.x0 = s.real();
