@@ -98,9 +98,10 @@ struct LightCurveIRS {
   // getLCIRS without the amoeba dump: joins concurrent calls of other objects
   // into one launch (same results as runFill)
   void runBatched(std::complex<double> s, std::complex<double> e);
-  // results of an object whose parameters the lens set-up cannot use: zero
-  // counts and magnifications, status bit 32 on every point
-  void badInputResults();
+  // results of an object kept off the GPU (parameters the lens set-up cannot
+  // use, or a set-up without device memory): zero counts and magnifications,
+  // its status (32 or 0x100) on every point
+  void unusableResults();
 
  private:
   // A, B and the intensity coefficient into the object and its device lens;

@@ -223,7 +223,7 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
     P.nseg = b->nseg;
     P.prep = (tl::PointPrep*)b->prep.p;
     P.chains = (tl::RootChain*)b->chains.p;
-    E.pipeline_exact(R, (size_t)b->npoints, P, b->precision, st);
+    if (!E.pipeline_exact(R, (size_t)b->npoints, P, b->precision, st)) return -2;
     return E.check(cudaGetLastError()) ? 0 : -2;
   }
   if (phase & 2) {
@@ -237,7 +237,8 @@ int tlb_run_device(tl_batch* b, int phase, void* stream) {
     R.dump = nullptr;
     R.dump_count = nullptr;
     R.dump_cap = 0;
-    E.fill_on(R, (size_t)b->npoints, (const tl::DevLens*)b->lenses.p, b->precision, st);
+    if (!E.fill_on(R, (size_t)b->npoints, (const tl::DevLens*)b->lenses.p, b->precision, st))
+      return -2;
   }
   return E.check(cudaGetLastError()) ? 0 : -2;
 }
@@ -338,9 +339,13 @@ int tlb_autotune(tl_batch* b, long sample_points, int32_t* chosen3, float* times
       R.dump_cap = 0;
       for (int rep = 0; rep < 2; rep++) {   // the first run allocates the tables
         cudaEventRecord(e0, E.stream);
-        E.fill_on(R, (size_t)np, (const tl::DevLens*)b->lenses.p, b->precision, E.stream);
+        const bool ran =
+            E.fill_on(R, (size_t)np, (const tl::DevLens*)b->lenses.p, b->precision, E.stream);
         cudaEventRecord(e1, E.stream);
-        if (!E.check(cudaEventSynchronize(e1))) break;
+        if (!E.check(cudaEventSynchronize(e1)) || !ran) {
+          ms = -1.f;   // a candidate that cannot run is not chosen
+          break;
+        }
         cudaEventElapsedTime(&ms, e0, e1);
       }
     }

@@ -213,9 +213,15 @@ Run RunBufs::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t ns
   R.dump = nullptr;
   R.dump_count = nullptr;
   R.dump_cap = 0;
-  if (dump) {
+  R.ok = R.trajs && R.jobs && R.points && R.seeds && R.out && R.trials &&
+         (!nscan || (R.scan_jobs && R.prep));
+  if (dump && R.ok) {
     const size_t cap = 1u << 22;  // tiles
     char* b = (char*)this->dump.need(sizeof(uint32_t) * kDumpWords * cap + 16, st);
+    if (!b) {
+      R.ok = false;
+      return R;
+    }
     R.dump_count = (unsigned*)b;
     R.dump = (uint32_t*)(b + 16);
     R.dump_cap = (unsigned)cap;
@@ -229,17 +235,18 @@ Run Engine::prepare(size_t np, size_t ntraj, size_t njobs, bool dump, size_t nsc
   return run_.prepare(np, ntraj, njobs, dump, nscan, stream);
 }
 
-void Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
-  fill_on(R, np, d_lenses, mode, stream);
+bool Engine::fill(const Run& R, size_t np, const DevLens* d_lenses, int mode) {
+  return fill_on(R, np, d_lenses, mode, stream);
 }
 
-void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
+bool Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode, cudaStream_t st) {
   NvtxRange range("tl fill");
   const bool warp = warp_fill_ != 0;
   const bool team = warp && team_fill_ != 0;
-  if (warp && !ensure_wscratch()) return;
-  if (team && !ensure_tscratch()) return;
-  if (!team && !ensure_fill_scratch(0)) return;
+  if (!R.ok) return false;
+  if (warp && !ensure_wscratch()) return false;
+  if (team && !ensure_tscratch()) return false;
+  if (!team && !ensure_fill_scratch(0)) return false;
   // the tables are shared: start after the previous fill, on any stream (a
   // graph being captured is ordered at its launch instead)
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -249,6 +256,7 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
   // largest points first; in the CTA fill the head of the list goes to its
   // large tables
   char* ob = (char*)order_.need(sizeof(int32_t) * np + 1024);
+  if (!ob || !retry_.need(sizeof(int32_t) * np + 64)) return false;
   unsigned* order_meta = (unsigned*)ob;
   int32_t* order_list = (int32_t*)(ob + 1024);
   launch_order(R.points, (int)np, order_list, order_meta, big_units_, st);
@@ -267,15 +275,17 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     unsigned long long* wprof = nullptr;
     if (profiling) {
       wprof = (unsigned long long*)wprof_.need(8 * sizeof(unsigned long long));
-      cudaMemsetAsync(wprof, 0, 8 * sizeof(unsigned long long), st);
-      w.prof = wprof;
+      if (wprof) {
+        cudaMemsetAsync(wprof, 0, 8 * sizeof(unsigned long long), st);
+        w.prof = wprof;
+      }
     }
     {
       NvtxRange stage("tl warp fill");
       launch_wfill(R.points, (int)np, d_lenses, R.seeds, R.out, w, mode, st, order_list,
                    order_meta);
     }
-    if (profiling) {
+    if (profiling && wprof) {
       cudaEventRecord(pe[1], st);
       unsigned long long h[8];
       cudaMemcpyAsync(h, wprof, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -294,15 +304,17 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
     unsigned long long* prof = nullptr;
     if (profiling) {
       prof = (unsigned long long*)prof_.need(8 * sizeof(unsigned long long));
-      cudaMemsetAsync(prof, 0, 8 * sizeof(unsigned long long), st);
-      s.prof = prof;
+      if (prof) {
+        cudaMemsetAsync(prof, 0, 8 * sizeof(unsigned long long), st);
+        s.prof = prof;
+      }
     }
     {
       NvtxRange stage("tl cta fill");
       launch_fill(R.points, (int)np, d_lenses, R.seeds, R.out, s, mode, threads_, st,
                   order_list, order_meta);
     }
-    if (profiling) {
+    if (profiling && prof) {
       unsigned long long h[8];
       cudaMemcpyAsync(h, prof, sizeof(h), cudaMemcpyDeviceToHost, st);
       cudaStreamSynchronize(st);
@@ -332,6 +344,7 @@ void Engine::fill_on(const Run& R, size_t np, const DevLens* d_lenses, int mode,
   }
   if (!capturing) fill_mark(st);
   check(cudaGetLastError());
+  return true;
 }
 
 void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mode,
@@ -340,6 +353,7 @@ void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mod
   // the launches read their point count on the device, so no host round trip
   // is needed (a launch with an empty list exits at once)
   char* rb = (char*)retry_.need(sizeof(int32_t) * np + 64);
+  if (!rb) return;   // allocated by the caller already: not reached
   int32_t* list = (int32_t*)(rb + 64);
   unsigned* count = (unsigned*)rb;
   if (warp && team) {
@@ -368,17 +382,19 @@ void Engine::fill_rest(const Run& R, size_t np, const DevLens* d_lenses, int mod
   }
 }
 
-void Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode,
+bool Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode,
                             cudaStream_t st) {
   NvtxRange range("tl seeds and fill");
   const bool team = team_fill_ != 0;
-  if (!ensure_wscratch()) return;
-  if (team && !ensure_tscratch()) return;
-  if (!team && !ensure_fill_scratch(0)) return;
-  if (!side_ && !check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking))) return;
+  if (!R.ok || !P.prep || !P.chains) return false;
+  if (!ensure_wscratch()) return false;
+  if (team && !ensure_tscratch()) return false;
+  if (!team && !ensure_fill_scratch(0)) return false;
+  if (!retry_.need(sizeof(int32_t) * np + 64)) return false;
+  if (!side_ && !check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking))) return false;
   while ((int)seg_ev_.size() < P.nseg + 1) {
     cudaEvent_t e;
-    if (!check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return;
+    if (!check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
     seg_ev_.push_back(e);
   }
   fill_after(st);
@@ -446,6 +462,7 @@ void Engine::pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode
     cudaEventDestroy(tend);
   }
   check(cudaGetLastError());
+  return true;
 }
 
 void Engine::fill_after(cudaStream_t st) { check(cudaStreamWaitEvent(st, fill_done_, 0)); }

@@ -65,6 +65,7 @@ struct Run {
   uint32_t* dump;
   unsigned* dump_count;
   unsigned dump_cap;
+  bool ok = true;          // every buffer the run needs was allocated
 };
 
 // The per-call device buffers of a run (grow-only).  The engine keeps one
@@ -98,11 +99,13 @@ class Engine {
   // runs the fill kernel over the points of R.  Fills share the engine's
   // tables: each fill waits (on the device) for the previous one, whatever
   // stream either was launched on.  Call with `mu` held.
-  void fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
-  void fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
+  // Both return false, with nothing launched, when the fill's tables or
+  // work lists could not be allocated.
+  bool fill(const Run& R, size_t npoints, const DevLens* d_lenses, int mode);
+  bool fill_on(const Run& R, size_t npoints, const DevLens* d_lenses, int mode, cudaStream_t st);
   // seeds (exact chain, in segments) and fill overlapped on st and a side
-  // stream; the result is ordered on st
-  void pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode, cudaStream_t st);
+  // stream; the result is ordered on st (false as fill_on)
+  bool pipeline_exact(const Run& R, size_t np, const Pipeline& P, int mode, cudaStream_t st);
   // order work that uses the fill tables outside fill_on (a graph replay):
   // fill_after makes st wait for the last fill, fill_mark records st's work
   // as the last fill

@@ -49,9 +49,11 @@ struct LightCurveIRS::Impl {
   tl::DevBuf specbuf, ampbuf;
   bool failed = false;
   bool fresh = true;        // no get_lc_irs yet
-  // parameters the lens set-up cannot use: the object runs nothing on the
-  // GPU and its calls report status bit 32 (bad input)
+  // parameters the lens set-up cannot use (status 32, bad input), or a
+  // set-up whose device memory could not be had (0x100): the object runs
+  // nothing on the GPU, and its calls report invalid_status on every point
   bool invalid = false;
+  uint32_t invalid_status = tl::kStBadInput;
   bool ck(cudaError_t e) {
     if (e != cudaSuccess) {
       fprintf(stderr, "liblcirs: CUDA error %s\n", cudaGetErrorString(e));
@@ -86,6 +88,12 @@ void setup_object(LightCurveIRS* o) {
     I->ck(cudaMallocAsync(&I->d_chain, sizeof(tl::RootChain), I->st));
   }
   tl::LensSpec* d_spec = (tl::LensSpec*)I->specbuf.need(sizeof(tl::LensSpec), I->st);
+  if (I->failed || !I->d_lens || !I->d_cc || !I->d_ca || !I->d_chain || !d_spec) {
+    // no stream or device memory for the set-up: kept off the GPU
+    I->invalid = true;
+    I->invalid_status = 0x100u;
+    return;
+  }
   I->ck(tl::copy_async(d_spec, &I->spec, sizeof(tl::LensSpec), cudaMemcpyHostToDevice, I->st));
   {
     tl::NvtxRange range("tl lens set-up");
@@ -148,6 +156,11 @@ LightCurveIRS::LightCurveIRS(double a_, double b_, double th_, double m2_, doubl
   g_constructing.fetch_add(1);
   setup_object(this);
   g_constructing.fetch_sub(1);
+  if (impl->invalid) {   // the set-up could not run
+    lastStatus = impl->invalid_status;
+    impl->fresh = false;
+    g_fresh.fetch_sub(1);
+  }
 }
 
 LightCurveIRS::~LightCurveIRS() {
@@ -359,6 +372,11 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
   auto* dl = (tl::DevLens*)B.lenses.need(sizeof(tl::DevLens) * k, B.st);
   auto* dca = (cx*)B.ca.need(sizeof(cx) * tl::kBranches * tl::kCCLen * k, B.st);
   auto* dch = (tl::RootChain*)B.chains.need(sizeof(tl::RootChain) * k, B.st);
+  if (!R.ok || !dl || !dca || !dch) {   // device memory exhausted: launch nothing
+    fprintf(stderr, "liblcirs: device allocation for a batch of %d curves failed\n", k);
+    for (Request* q : reqs) q->obj->lastStatus = 0x100u;
+    return;
+  }
   // gather the objects' lenses, caustics and warm-start chains
   for (int i = 0; i < k; i++) {
     const LightCurveIRS::Impl* I = reqs[i]->obj->impl;
@@ -391,6 +409,11 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
     auto* dsj = (tl::SeedJob*)B.segjobs.need(sizeof(tl::SeedJob) * sj.size(), B.st);
     auto* dsl = (int32_t*)B.seglist.need(sizeof(int32_t) * sl.size(), B.st);
     auto* dsn = (unsigned*)B.segn.need(sizeof(unsigned) * S, B.st);
+    if (!dsj || !dsl || !dsn) {
+      fprintf(stderr, "liblcirs: device allocation for a batch of %d curves failed\n", k);
+      for (Request* q : reqs) q->obj->lastStatus = 0x100u;
+      return;
+    }
     ck(tl::copy_async(dsj, sj.data(), sizeof(tl::SeedJob) * sj.size(), cudaMemcpyHostToDevice,
                        B.st));
     ck(tl::copy_async(dsl, sl.data(), sizeof(int32_t) * sl.size(), cudaMemcpyHostToDevice,
@@ -412,12 +435,12 @@ void run_batch(Batcher& B, const std::vector<Request*>& reqs) {
     P.chains = dch;
     P.reset_chains = false;
     std::lock_guard<std::mutex> g(E.mu);
-    E.pipeline_exact(R, total, P, precision, B.st);
+    if (!E.pipeline_exact(R, total, P, precision, B.st)) failed = true;
   } else {
     tl::launch_seeds(R.jobs, (int)jobs.size(), R.trajs, dl, dca, R.points, R.seeds, R.out,
                      R.trials, dch, B.st);
     std::lock_guard<std::mutex> g(E.mu);
-    E.fill_on(R, total, dl, precision, B.st);
+    if (!E.fill_on(R, total, dl, precision, B.st)) failed = true;
   }
   // the chains go back to their objects
   for (int i = 0; i < k; i++)
@@ -493,23 +516,23 @@ void LightCurveIRS::runBatched(std::complex<double> s, std::complex<double> e) {
   }
 }
 
-void LightCurveIRS::badInputResults() {
+void LightCurveIRS::unusableResults() {
   const size_t np = (size_t)lcLength + 1;
   counts.assign(np, 0);
-  status.assign(np, tl::kStBadInput);
+  status.assign(np, impl->invalid_status);
   diag.assign(np, 0);
   nseeds.assign(np, 0);
   seeds.assign(np * 2 * tl::kMaxSeeds, 0);
   for (double& v : lcVec) v = 0.0;
   for (double& v : impl->lcFull) v = 0.0;
   stats[0] = stats[1] = stats[2] = 0;
-  lastStatus = tl::kStBadInput;
+  lastStatus = impl->invalid_status;
 }
 
 void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
                             const int32_t* extSeeds, const int32_t* extN) {
   if (impl->invalid) {
-    badInputResults();
+    unusableResults();
     return;
   }
   tl::Engine& E = tl::Engine::get();
@@ -530,6 +553,11 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   if (chainPoints <= 0) tl::plan_jobs(&scan, 0, (long)np, tl::kChainChunk, -1);
   E.trace("runFill: prepare");
   tl::Run R = I->bufs.prepare(np, 1, jobs.size(), amoebaPrintOut_, scan.size(), I->st);
+  if (!R.ok) {   // device memory exhausted: launch nothing
+    I->failed = true;
+    lastStatus = 0x100u;
+    return;
+  }
   I->ck(tl::copy_async(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
   I->ck(tl::copy_async(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, I->st));
@@ -567,7 +595,7 @@ void LightCurveIRS::runFill(std::complex<double> s, std::complex<double> e,
   {
     // the fill tables are the engine's: one launch sequence at a time
     std::lock_guard<std::mutex> g(E.mu);
-    E.fill_on(R, np, impl->d_lens, precision, I->st);
+    if (!E.fill_on(R, np, impl->d_lens, precision, I->st)) I->failed = true;
   }
   E.trace("runFill: fill launched");
   if (E.sync_steps) {
@@ -645,7 +673,7 @@ void LightCurveIRS::getLCIRS(std::complex<double> s, std::complex<double> e) {
     g_fresh.fetch_sub(1);
   }
   if (impl->invalid) {
-    badInputResults();
+    unusableResults();
     return;
   }
   if (amoebaPrintOut_) {
@@ -662,7 +690,7 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   if (I->invalid) {
     for (double& v : lcVec) v = 0.0;
     for (double& v : I->lcFull) v = 0.0;
-    lastStatus = tl::kStBadInput;
+    lastStatus = I->invalid_status;
     return;
   }
   if (n == 0) return;
@@ -677,10 +705,18 @@ void LightCurveIRS::getLC(std::complex<double> s, std::complex<double> e) {
   std::vector<tl::SeedJob> jobs;
   tl::plan_jobs(&jobs, 0, (long)n, chainPoints, 0);
   tl::Run R = I->bufs.prepare(n, 1, jobs.size(), false, 0, I->st);
+  if (!R.ok) {   // device memory exhausted: launch nothing
+    lastStatus = 0x100u;
+    return;
+  }
   I->ck(tl::copy_async(R.trajs, &T, sizeof(T), cudaMemcpyHostToDevice, I->st));
   I->ck(tl::copy_async(R.jobs, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, I->st));
   double* d_amp = (double*)I->ampbuf.need(sizeof(double) * n, I->st);
+  if (!d_amp) {   // device memory exhausted: launch nothing
+    lastStatus = 0x100u;
+    return;
+  }
   if (chainPoints <= 0)
     tl::launch_point_lc_exact(R.trajs, R.jobs, (int)jobs.size(), impl->d_lens, d_amp,
                               impl->d_chain, I->st);
