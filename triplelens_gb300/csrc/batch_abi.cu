@@ -431,7 +431,10 @@ static long point_lc_body(tl_batch* b, double* amp) {
   tl::DevBuf dj;
   void* djp = dj.need(sizeof(tl::SeedJob) * jobs.size());
   double* da = (double*)b->amp.need(sizeof(double) * b->npoints);
-  if (!djp || !da) return -2;
+  if (!djp || !da) {
+    if (djp) cudaFree(djp);
+    return -2;
+  }
   E.check(cudaMemsetAsync(da, 0, sizeof(double) * b->npoints, E.stream));
   E.check(tl::copy_async(djp, jobs.data(), sizeof(tl::SeedJob) * jobs.size(),
                           cudaMemcpyHostToDevice, E.stream));
