@@ -161,8 +161,14 @@ int main() {
   for (int rep = 0; rep < 3; rep++) {
     Sim s;
     std::vector<std::thread> th;
+    std::atomic<int> ready{0};   // every thread exists before any set-up starts
     for (int k = 0; k < 152; k++)
-      th.emplace_back([&s, k] { s.construct(k == 0 ? 22 : 32); s.call(20); });
+      th.emplace_back([&s, &ready, k] {
+        ready++;
+        while (ready.load() < 152) std::this_thread::yield();
+        s.construct(k == 0 ? 22 : 32);
+        s.call(20);
+      });
     for (auto& t : th) t.join();
     if (s.batches.size() != 1 || s.batches[0] != 152) {
       printf("FAIL pool: %zu batches, first %zu\n", s.batches.size(), s.batches[0]);
