@@ -44,6 +44,20 @@ def test_plan_is_deterministic_and_rejects_bad_costs():
         shard.plan([1.0], 0)
 
 
+def test_plan_with_more_ranks_than_curves_and_zero_costs():
+    """Ranks beyond the number of curves get empty shares (ShardedCurves
+    skips their predictor and runner calls); zero-cost curves are still
+    assigned, and every curve exactly once."""
+    shares = shard.plan([3.0, 0.0, 1.0], 8)
+    assert len(shares) == 8
+    assert sorted(np.concatenate(shares).tolist()) == [0, 1, 2]
+    assert sum(len(s) == 0 for s in shares) == 5
+    shares = shard.plan(np.zeros(10), 3)
+    assert sorted(np.concatenate(shares).tolist()) == list(range(10))
+    assert [len(s) for s in shares] == [4, 3, 3]
+    assert shard.plan([], 2)[0].size == 0
+
+
 def test_predicted_rays_from_point_magnifications():
     lenses = np.array([[1, 1, 0, 0.1, 0.1, 1e-3, 0.5, 500.0],
                        [1, 1, 0, 0.1, 0.1, 1e-3, 0.5, 100.0]])

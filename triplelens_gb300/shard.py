@@ -41,7 +41,9 @@ def plan(costs, world):
     loads = [0.0] * world
     shares = [[] for _ in range(world)]
     for i in order:
-        r = min(range(world), key=lambda k: (loads[k], k))
+        # least loaded rank; on equal loads the one with fewer curves (zero
+        # or equal costs then go round-robin, not all to the first rank)
+        r = min(range(world), key=lambda k: (loads[k], len(shares[k]), k))
         shares[r].append(int(i))
         loads[r] += float(costs[i])
     return [np.array(sorted(s), dtype=np.int64) for s in shares]
